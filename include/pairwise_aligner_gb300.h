@@ -1,0 +1,169 @@
+/*
+ * pairwise_aligner_gb300.h -- C ABI of the GB300 (sm_103a) affine-gap score DP.
+ *
+ * The reference library (rrahn/pairwise_aligner) is header-only C++20 and has no
+ * FFI; its plug point for this path is the score-model rule category
+ * (include/pairwise_aligner/configuration/rule_category.hpp:24-30) whose traits
+ * return the interface object, and the call a user makes is
+ *     auto a = cfg::configure_aligner(cfg::method_global(cfg::gap_model_affine(
+ *                  cfg::score_model_unitary_simd_saturated(match, mismatch), open, ext), lead, trail));
+ *     for (auto r : a.compute(seqs1, seqs2)) r.score();
+ * (test/unit/configuration/configure_aligner_saturated_test.cpp:22-41).  The
+ * entry points below are what that interface object's compute() binds to in
+ * this project: pairwise_aligner_gb300.hpp (header-only C++20, same cfg::
+ * names) and pairwise_aligner_gb300/ (Python) call them.
+ *
+ * Conventions shared by every entry point:
+ *  - Plain pointers and sizes only.  Sequences are concatenated bytes plus
+ *    n_pairs+1 uint64 offsets (pair k is bytes [off[k], off[k+1])).  Bytes are
+ *    compared raw, like score_model_unitary::score (score_model_unitary.hpp:52-59).
+ *  - Scores use the reference's signs: match > 0, mismatch < 0, gap_open <= 0,
+ *    gap_extension <= 0; a gap of length k scores gap_open + k * gap_extension
+ *    (affine_initialisation_strategy.hpp:38-51, affine_dp_algorithm.hpp:149-155).
+ *  - Errors are status codes; nothing throws across the ABI.
+ *  - One context per host thread (or external locking).  A context owns one
+ *    CUDA stream, its device buffers and its CUDA-graph cache.
+ */
+#ifndef PAIRWISE_ALIGNER_GB300_H
+#define PAIRWISE_ALIGNER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PA_ABI_VERSION 1
+
+typedef enum pa_status {
+    PA_OK = 0,
+    PA_ERR_INVALID_ARGUMENT = 1,  /* null pointer, bad offsets, bad config            */
+    PA_ERR_CUDA = 2,              /* a CUDA runtime call failed (see pa_last_error)    */
+    PA_ERR_OUT_OF_MEMORY = 3,
+    PA_ERR_OVERFLOW = 4,          /* scores could exceed int32 for this input          */
+    PA_ERR_UNSUPPORTED = 5,       /* e.g. a positive gap score                         */
+    PA_ERR_TIMEOUT = 6,           /* a bounded device-side wait gave up                */
+    PA_ERR_NO_DEVICE = 7,
+    PA_ERR_TOO_LARGE = 8          /* sizes beyond a fixed capacity                     */
+} pa_status;
+
+typedef enum pa_method { PA_METHOD_GLOBAL = 0, PA_METHOD_LOCAL = 1 } pa_method;
+
+/* Alignment configuration.  Replaces the compile-time rule chain
+ * cfg::method_global / cfg::method_local (method_global.hpp:121-145,
+ * method_local.hpp:118-137), cfg::gap_model_affine (gap_model_affine.hpp:130-155)
+ * and cfg::score_model_unitary* (score_model_unitary_simd_saturated.hpp:259-284).
+ * The end-gap flags follow cfg::leading_end_gap / cfg::trailing_end_gap
+ * (end_gap_policy.hpp:26-36); method_local forces all four free. */
+typedef struct pa_config {
+    int32_t method;             /* pa_method                                              */
+    int32_t match;
+    int32_t mismatch;
+    int32_t gap_open;
+    int32_t gap_extension;
+    uint8_t first_column_free;  /* leading gap in sequence1 free: H(i,0) = 0              */
+    uint8_t first_row_free;     /* leading gap in sequence2 free: H(0,j) = 0              */
+    uint8_t last_column_free;   /* the result may end anywhere in column n                */
+    uint8_t last_row_free;      /* the result may end anywhere in row m                   */
+    int32_t width_hint;         /* 0 auto (s16x2 then s32), 16, or 32                     */
+    int32_t band_mode;          /* 0: plain full DP.  1: learned band + certificate       */
+} pa_config;
+
+/* Per-pair result (16 bytes).  score mirrors aligner_result::score()
+ * (result/aligner_result.hpp:32-105); end1/end2 are 1-based end positions in
+ * sequence1/sequence2 (the reference has none: "TODO: optimal_coordinate()"),
+ * ties to the smallest end1, then the smallest end2.  Local: a score of 0 gives
+ * (0,0); an empty sequence gives INT32_MIN and (0,0), like
+ * tracker_local_scalar.hpp:38. */
+typedef struct pa_result {
+    int32_t score;
+    int32_t end1;
+    int32_t end2;
+    uint8_t width;              /* 16 or 32: arithmetic width that produced the score      */
+    uint8_t flags;              /* PA_RESULT_* bits                                        */
+    uint16_t band_rounds;       /* band doublings used (band_mode 1), else 0               */
+} pa_result;
+
+#define PA_RESULT_RERUN      0x01u  /* s16 result failed its exactness check, rerun at s32 */
+#define PA_RESULT_BANDED     0x02u  /* certified banded result                              */
+#define PA_RESULT_FULL_DP    0x04u  /* band fell back to the full DP                        */
+#define PA_RESULT_TRIVIAL    0x08u  /* an empty sequence: answered without a DP             */
+
+/* Context options; zero-initialised means defaults. */
+typedef struct pa_options {
+    int32_t group_threads;      /* threads per pair group: 0 auto, else 1,2,4,8,16,32      */
+    int32_t rows_per_thread;    /* rows a thread holds per lane: 0 auto, else 8,16,32      */
+    int32_t blocks_per_sm;      /* persistent grid occupancy: 0 auto                       */
+    int32_t use_graphs;         /* 0 auto(on), 1 on, -1 off                                */
+    int32_t autotune;           /* 0 off, 1 on first use                                   */
+    int32_t reserved[3];
+} pa_options;
+
+/* Counters of the last call. */
+typedef struct pa_stats {
+    uint64_t pairs;
+    uint64_t cells;             /* sum of m*n over pairs (full-matrix cells)              */
+    uint64_t pairs_s16;         /* pairs finished in s16x2 lanes                          */
+    uint64_t pairs_s32;         /* pairs finished in s32 lanes (incl. reruns)             */
+    uint64_t pairs_general;     /* pairs whose sequence2 is not all A/C/G/T               */
+    uint64_t pairs_rerun;       /* s16 results promoted to s32                            */
+    uint64_t pairs_trivial;
+    uint64_t kernel_launches;   /* kernels this call launched                             */
+    double   device_ms;         /* device time of the whole call (CUDA events)            */
+    double   dp_ms;             /* device time of the DP kernels alone                    */
+} pa_stats;
+
+typedef struct pa_ctx pa_ctx;
+
+/* Create / destroy a context bound to a CUDA device ordinal. */
+pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options);
+pa_status pa_destroy(pa_ctx *ctx);
+
+/* Align n_pairs pairs given in HOST memory; synchronous.  Replaces
+ * interface_one_to_one_bulk::compute (interface/interface_one_to_one_bulk.hpp:47-100)
+ * without its "<= lane count" batch limit (:55-57): any n_pairs.  Host buffers
+ * may be pageable or pinned; out has n_pairs entries.  stats may be NULL. */
+pa_status pa_align_batch(pa_ctx *ctx, const pa_config *config,
+                         const uint8_t *seq1, const uint64_t *off1,
+                         const uint8_t *seq2, const uint64_t *off2,
+                         uint64_t n_pairs, pa_result *out, pa_stats *stats);
+
+/* Same, with every buffer already in device memory of the context's device.
+ * Asynchronous on `stream` (a cudaStream_t; NULL = the context's stream,
+ * cudaStreamLegacy / cudaStreamPerThread are accepted);
+ * seq1_bytes / seq2_bytes are the sizes of the two byte buffers.  When stats
+ * is non-NULL the call synchronises to fill it. */
+pa_status pa_align_batch_device(pa_ctx *ctx, const pa_config *config,
+                                const uint8_t *d_seq1, const uint64_t *d_off1, uint64_t seq1_bytes,
+                                const uint8_t *d_seq2, const uint64_t *d_off2, uint64_t seq2_bytes,
+                                uint64_t n_pairs, pa_result *d_out, void *stream, pa_stats *stats);
+
+/* One query against many targets (interface/interface_one_to_many_bulk.hpp:47-92):
+ * pair k is (query, targets[k]).  Host buffers, synchronous. */
+pa_status pa_align_one_to_many(pa_ctx *ctx, const pa_config *config,
+                               const uint8_t *query, uint64_t query_len,
+                               const uint8_t *targets, const uint64_t *target_off,
+                               uint64_t n_targets, pa_result *out, pa_stats *stats);
+
+/* Measured whole-chip throughput of the cell-update instruction mix, used as
+ * the roofline denominator: packed s16x2 DPX cell updates per second and s32
+ * cell updates per second, from a timed in-register microkernel. */
+typedef struct pa_roofline {
+    double s16x2_cells_per_s;
+    double s32_cells_per_s;
+    double sm_clock_mhz;
+    int32_t sm_count;
+    int32_t reserved;
+} pa_roofline;
+pa_status pa_measure_roofline(pa_ctx *ctx, pa_roofline *out);
+
+const char *pa_status_string(pa_status status);
+/* Message of the last error on this context (empty string if none). */
+const char *pa_last_error(const pa_ctx *ctx);
+int pa_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PAIRWISE_ALIGNER_GB300_H */

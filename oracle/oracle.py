@@ -1,0 +1,135 @@
+"""ctypes front of the CPU oracle (oracle/pa_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the checker the GPU path is compared with.  Only
+tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline / reference
+legs import this module.  The product package never does.
+
+The C file restates the reference's scalar path (see its header for the
+file:line citations); this module only builds and loads it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "pa_oracle.c")
+_LIB = os.path.join(_HERE, "liboracle.so")
+_lock = threading.Lock()
+_lib = None
+
+
+class OracleCfg(ctypes.Structure):
+    _fields_ = [
+        ("match", ctypes.c_int32),
+        ("mismatch", ctypes.c_int32),
+        ("gap_open", ctypes.c_int32),
+        ("gap_extension", ctypes.c_int32),
+        ("local", ctypes.c_int32),
+        ("first_column_free", ctypes.c_int32),
+        ("first_row_free", ctypes.c_int32),
+        ("last_column_free", ctypes.c_int32),
+        ("last_row_free", ctypes.c_int32),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile oracle/pa_oracle.c into oracle/liboracle.so (portable flags, no -march)."""
+    with _lock:
+        if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):
+            cmd = ["gcc", "-O3", "-std=c11", "-Wall", "-Wextra", "-Wno-psabi", "-fPIC", "-shared",
+                   "-pthread", _SRC, "-o", _LIB + ".tmp"]
+            subprocess.check_call(cmd)
+            os.replace(_LIB + ".tmp", _LIB)
+    return _LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB)
+        u8p = ctypes.POINTER(ctypes.c_uint8)
+        u64p = ctypes.POINTER(ctypes.c_uint64)
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        L.pa_oracle_align.argtypes = [ctypes.POINTER(OracleCfg), u8p, ctypes.c_uint64, u8p, ctypes.c_uint64,
+                                      i64p, i64p, i64p]
+        L.pa_oracle_align.restype = ctypes.c_int
+        L.pa_oracle_align_batch.argtypes = [ctypes.POINTER(OracleCfg), u8p, u64p, u8p, u64p, ctypes.c_uint64,
+                                            i64p, i64p, i64p, ctypes.c_int]
+        L.pa_oracle_align_batch.restype = ctypes.c_int
+        L.pa_oracle_simd_batch.argtypes = [ctypes.POINTER(OracleCfg), u8p, u64p, u8p, u64p, ctypes.c_uint64,
+                                           i32p, ctypes.c_int]
+        L.pa_oracle_simd_batch.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def make_cfg(match, mismatch, gap_open, gap_extension, local=False, first_column_free=False,
+             first_row_free=False, last_column_free=False, last_row_free=False) -> OracleCfg:
+    return OracleCfg(int(match), int(mismatch), int(gap_open), int(gap_extension), int(bool(local)),
+                     int(bool(first_column_free)), int(bool(first_row_free)), int(bool(last_column_free)),
+                     int(bool(last_row_free)))
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def align(cfg: OracleCfg, s1: bytes, s2: bytes):
+    """One pair -> (score, end1, end2)."""
+    a = np.frombuffer(bytes(s1), dtype=np.uint8) if len(s1) else np.zeros(1, np.uint8)
+    b = np.frombuffer(bytes(s2), dtype=np.uint8) if len(s2) else np.zeros(1, np.uint8)
+    sc, e1, e2 = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    rc = lib().pa_oracle_align(ctypes.byref(cfg), _ptr(a, ctypes.c_uint8), len(s1), _ptr(b, ctypes.c_uint8),
+                               len(s2), ctypes.byref(sc), ctypes.byref(e1), ctypes.byref(e2))
+    if rc:
+        raise RuntimeError(f"pa_oracle_align failed: {rc}")
+    return sc.value, e1.value, e2.value
+
+
+def align_batch(cfg: OracleCfg, s1: np.ndarray, off1: np.ndarray, s2: np.ndarray, off2: np.ndarray,
+                nthreads: int | None = None):
+    """Batch over concatenated bytes + (n_pairs+1) uint64 offsets -> (scores, end1, end2) int64 arrays."""
+    n = len(off1) - 1
+    s1 = np.ascontiguousarray(s1, dtype=np.uint8)
+    s2 = np.ascontiguousarray(s2, dtype=np.uint8)
+    off1 = np.ascontiguousarray(off1, dtype=np.uint64)
+    off2 = np.ascontiguousarray(off2, dtype=np.uint64)
+    if s1.size == 0:
+        s1 = np.zeros(1, np.uint8)
+    if s2.size == 0:
+        s2 = np.zeros(1, np.uint8)
+    scores = np.empty(n, np.int64)
+    e1 = np.empty(n, np.int64)
+    e2 = np.empty(n, np.int64)
+    nt = nthreads or os.cpu_count() or 1
+    rc = lib().pa_oracle_align_batch(ctypes.byref(cfg), _ptr(s1, ctypes.c_uint8), _ptr(off1, ctypes.c_uint64),
+                                     _ptr(s2, ctypes.c_uint8), _ptr(off2, ctypes.c_uint64), n,
+                                     _ptr(scores, ctypes.c_int64), _ptr(e1, ctypes.c_int64),
+                                     _ptr(e2, ctypes.c_int64), nt)
+    if rc:
+        raise RuntimeError(f"pa_oracle_align_batch failed: {rc}")
+    return scores, e1, e2
+
+
+def simd_batch(cfg: OracleCfg, s1, off1, s2, off2, nthreads: int | None = None) -> np.ndarray:
+    """Inter-sequence int16-lane SIMD port (scores only) -- the timed CPU baseline."""
+    n = len(off1) - 1
+    s1 = np.ascontiguousarray(s1, dtype=np.uint8)
+    s2 = np.ascontiguousarray(s2, dtype=np.uint8)
+    off1 = np.ascontiguousarray(off1, dtype=np.uint64)
+    off2 = np.ascontiguousarray(off2, dtype=np.uint64)
+    scores = np.empty(max(n, 1), np.int32)
+    nt = nthreads or os.cpu_count() or 1
+    rc = lib().pa_oracle_simd_batch(ctypes.byref(cfg), _ptr(s1, ctypes.c_uint8), _ptr(off1, ctypes.c_uint64),
+                                    _ptr(s2, ctypes.c_uint8), _ptr(off2, ctypes.c_uint64), n,
+                                    _ptr(scores, ctypes.c_int32), nt)
+    if rc:
+        raise RuntimeError(f"pa_oracle_simd_batch failed: {rc}")
+    return scores[:n]

@@ -1,0 +1,396 @@
+/*
+ * pa_oracle.c -- CPU oracle for the affine-gap (Gotoh) score-only pairwise alignment.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU path is compared
+ * against; it is never part of the product path.  Only tests/, the smoke()
+ * check in __graft_entry__.py and bench.py's CPU-baseline / reference legs may
+ * load it.  The product library (pairwise_aligner_gb300) does not link it and
+ * fails loudly when its own CUDA library is missing.
+ *
+ * Two entry families:
+ *
+ *  1. pa_oracle_align / pa_oracle_align_batch -- a scalar restatement of the
+ *     reference's scalar path (cfg::score_model_unitary), int64 internally,
+ *     plus end coordinates under this project's tie-break convention.
+ *       - recurrence: include/pairwise_aligner/affine/affine_dp_algorithm.hpp:133-156
+ *       - border cells: include/pairwise_aligner/affine/affine_initialisation_strategy.hpp:38-51
+ *       - local clamp of the diagonal term: include/pairwise_aligner/matrix/dp_matrix_local.hpp:39-47
+ *       - substitution: include/pairwise_aligner/score_model/score_model_unitary.hpp:52-59
+ *       - global result (+ free trailing row/column): include/pairwise_aligner/tracker/tracker_global_scalar.hpp:36-61
+ *       - local result (max over all cells, lowest() when empty): include/pairwise_aligner/tracker/tracker_local_scalar.hpp:38-49
+ *     Parity is pinned against the reference's hand-written golden scores
+ *     (the test/unit/affine scalar tests) by tests/test_oracle_golden.py.
+ *
+ *  2. pa_oracle_simd_batch -- a multi-threaded inter-sequence SIMD port of the
+ *     reference's fixed-width SIMD path (cfg::score_model_unitary_simd,
+ *     include/pairwise_aligner/configuration/score_model_unitary_simd.hpp:51-137):
+ *     one alignment per int16 vector lane, GCC vector extensions (portable to
+ *     x86 SSE and Arm NEON), pthreads over batches.  Scores only, like the
+ *     reference.  It is the timed CPU baseline where the reference itself can
+ *     not be built.
+ *
+ * End-coordinate convention (the reference computes none: every tracker has
+ * "TODO: optimal_coordinate()"): 1-based (i, j) = (end in sequence1, end in
+ * sequence2) of the best cell; ties go to the smallest i, then the smallest j.
+ * Local: a best score of 0 reports (0, 0); an empty input reports INT32_MIN and
+ * (0, 0).  Global: the candidate cells are (m, n), plus the last row (m, 0..n)
+ * when the trailing row gap is free, plus the last column (0..m, n) when the
+ * trailing column gap is free.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <pthread.h>
+
+#define PA_ORACLE_OK 0
+#define PA_ORACLE_EINVAL 1
+#define PA_ORACLE_ENOMEM 2
+
+typedef struct pa_oracle_cfg {
+    int32_t match;              /* score of a == b                       */
+    int32_t mismatch;           /* score of a != b                       */
+    int32_t gap_open;           /* gap of length k scores open + k * ext */
+    int32_t gap_extension;
+    int32_t local;              /* 1: method_local (all end gaps free)   */
+    int32_t first_column_free;  /* leading gap in sequence1 free (H(i,0) = 0) */
+    int32_t first_row_free;     /* leading gap in sequence2 free (H(0,j) = 0) */
+    int32_t last_column_free;   /* result may end in column n            */
+    int32_t last_row_free;      /* result may end in row m               */
+} pa_oracle_cfg;
+
+static inline int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
+
+/* Border cell k of the first row (order = row) or first column (order = column).
+ * Index 0 -> (0, open+ext); k > 0 penalised -> (open + ext*k, that + open + ext);
+ * free -> (0, open+ext).   affine_initialisation_strategy.hpp:38-51 */
+static inline void border_cell(const pa_oracle_cfg *c, int free_rule, uint64_t k, int64_t *h, int64_t *gap)
+{
+    int64_t goe = (int64_t)c->gap_open + c->gap_extension;
+    int64_t first = 0;
+    if (!free_rule && k > 0)
+        first = (int64_t)c->gap_open + (int64_t)c->gap_extension * (int64_t)k;
+    *h = first;
+    *gap = first + goe;
+}
+
+/* Scalar Gotoh.  Rows i run over sequence1 (the reference's "column sequence"),
+ * columns j over sequence2.  vgap[j] is the vertical gap carried down column j
+ * (the reference's row-cell .second); hgap is the horizontal gap carried along
+ * row i (the reference's column-cell .second).  affine_dp_algorithm.hpp:149-155 */
+int pa_oracle_align(const pa_oracle_cfg *c, const uint8_t *s1, uint64_t m, const uint8_t *s2, uint64_t n,
+                    int64_t *score, int64_t *end1, int64_t *end2)
+{
+    if (!c || !score || !end1 || !end2) return PA_ORACLE_EINVAL;
+    const int local = c->local != 0;
+    const int first_col_free = local || c->first_column_free;
+    const int first_row_free = local || c->first_row_free;
+    const int last_col_free = !local && c->last_column_free;
+    const int last_row_free = !local && c->last_row_free;
+    const int64_t goe = (int64_t)c->gap_open + c->gap_extension;
+    const int64_t ext = c->gap_extension;
+
+    int64_t *hrow = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
+    int64_t *vgap = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
+    if (!hrow || !vgap) { free(hrow); free(vgap); return PA_ORACLE_ENOMEM; }
+    for (uint64_t j = 0; j <= n; ++j) border_cell(c, first_row_free, j, &hrow[j], &vgap[j]);
+
+    /* result bookkeeping */
+    int64_t best = INT64_MIN, bi = 0, bj = 0;
+    int have = 0;
+    if (!local) {
+        if (last_col_free) { best = hrow[n]; bi = 0; bj = n; have = 1; }  /* H(0, n) */
+        if (m == 0) {                                                       /* H(0, n) is the corner */
+            if (!have || hrow[n] > best) { best = hrow[n]; bi = 0; bj = n; }
+            have = 1;
+            if (last_row_free)                                              /* row m = 0 */
+                for (uint64_t j = 0; j <= n; ++j)
+                    if (hrow[j] > best || (hrow[j] == best && (0 < bi || (0 == bi && (int64_t)j < bj)))) {
+                        best = hrow[j]; bi = 0; bj = (int64_t)j;
+                    }
+        }
+    }
+
+    for (uint64_t i = 1; i <= m; ++i) {
+        int64_t hc, hgap;
+        border_cell(c, first_col_free, i, &hc, &hgap);
+        int64_t diag = hrow[0];
+        hrow[0] = hc;
+        const uint8_t a = s1[i - 1];
+        for (uint64_t j = 1; j <= n; ++j) {
+            int64_t d = diag + ((a == s2[j - 1]) ? c->match : c->mismatch);
+            if (local) d = max64(d, 0);                       /* dp_matrix_local.hpp:39-47 */
+            int64_t h = max64(max64(d, vgap[j]), hgap);
+            diag = hrow[j];
+            hrow[j] = h;
+            if (local && h > best) { best = h; bi = (int64_t)i; bj = (int64_t)j; }
+            int64_t hoe = h + goe;
+            vgap[j] = max64(vgap[j] + ext, hoe);
+            hgap = max64(hgap + ext, hoe);
+        }
+        if (!local && last_col_free) {                       /* H(i, n); (i, n) beats later rows on ties */
+            if (hrow[n] > best) { best = hrow[n]; bi = (int64_t)i; bj = (int64_t)n; }
+        }
+    }
+
+    if (local) {
+        if (m == 0 || n == 0) { *score = INT32_MIN; *end1 = 0; *end2 = 0; }   /* tracker_local_scalar.hpp:38 */
+        else if (best <= 0) { *score = best; *end1 = 0; *end2 = 0; }
+        else { *score = best; *end1 = bi; *end2 = bj; }
+    } else {
+        if (m > 0) {
+            /* (m, n) and, with a free trailing row, the last row (m, 0..n). */
+            if (last_row_free) {
+                for (uint64_t j = 0; j <= n; ++j) {
+                    int better = !have || hrow[j] > best ||
+                                 (hrow[j] == best && ((int64_t)m < bi || ((int64_t)m == bi && (int64_t)j < bj)));
+                    if (better) { best = hrow[j]; bi = (int64_t)m; bj = (int64_t)j; have = 1; }
+                }
+            } else {
+                int better = !have || hrow[n] > best ||
+                             (hrow[n] == best && ((int64_t)m < bi || ((int64_t)m == bi && (int64_t)n < bj)));
+                if (better) { best = hrow[n]; bi = (int64_t)m; bj = (int64_t)n; have = 1; }
+            }
+        }
+        *score = best; *end1 = bi; *end2 = bj;
+    }
+    free(hrow); free(vgap);
+    return PA_ORACLE_OK;
+}
+
+/* ------------------------------------------------------------------------- */
+/* batch driver over (bytes, offsets) -- the same layout the C-ABI takes       */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+    const pa_oracle_cfg *cfg;
+    const uint8_t *s1; const uint64_t *off1;
+    const uint8_t *s2; const uint64_t *off2;
+    uint64_t begin, end, stride;
+    int64_t *scores, *end1, *end2;
+    int rc;
+} scalar_job;
+
+static void *scalar_worker(void *p)
+{
+    scalar_job *jb = (scalar_job *)p;
+    for (uint64_t k = jb->begin; k < jb->end; k += jb->stride) {
+        int64_t sc, e1, e2;
+        int rc = pa_oracle_align(jb->cfg, jb->s1 + jb->off1[k], jb->off1[k + 1] - jb->off1[k],
+                                 jb->s2 + jb->off2[k], jb->off2[k + 1] - jb->off2[k], &sc, &e1, &e2);
+        if (rc) { jb->rc = rc; return NULL; }
+        jb->scores[k] = sc;
+        if (jb->end1) jb->end1[k] = e1;
+        if (jb->end2) jb->end2[k] = e2;
+    }
+    return NULL;
+}
+
+int pa_oracle_align_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint64_t *off1,
+                          const uint8_t *s2, const uint64_t *off2, uint64_t n_pairs,
+                          int64_t *scores, int64_t *end1, int64_t *end2, int nthreads)
+{
+    if (!c || !scores || (n_pairs && (!off1 || !off2))) return PA_ORACLE_EINVAL;
+    if (nthreads < 1) nthreads = 1;
+    if ((uint64_t)nthreads > n_pairs) nthreads = n_pairs ? (int)n_pairs : 1;
+    scalar_job *jobs = (scalar_job *)calloc((size_t)nthreads, sizeof(scalar_job));
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!jobs || !th) { free(jobs); free(th); return PA_ORACLE_ENOMEM; }
+    for (int t = 0; t < nthreads; ++t) {
+        jobs[t] = (scalar_job){c, s1, off1, s2, off2, (uint64_t)t, n_pairs, (uint64_t)nthreads,
+                               scores, end1, end2, 0};
+    }
+    for (int t = 1; t < nthreads; ++t) pthread_create(&th[t], NULL, scalar_worker, &jobs[t]);
+    scalar_worker(&jobs[0]);
+    int rc = jobs[0].rc;
+    for (int t = 1; t < nthreads; ++t) { pthread_join(th[t], NULL); if (jobs[t].rc) rc = jobs[t].rc; }
+    free(jobs); free(th);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------- */
+/* inter-sequence SIMD port (CPU baseline), scores only                        */
+/* ------------------------------------------------------------------------- */
+
+#define PA_LANES 16
+typedef int16_t v16s __attribute__((vector_size(32)));
+
+static inline v16s vsel(v16s mask, v16s a, v16s b) { return (a & mask) | (b & ~mask); }
+static inline v16s vmax(v16s a, v16s b) { return vsel((v16s)(a > b), a, b); }
+
+typedef struct {
+    const pa_oracle_cfg *cfg;
+    const uint8_t *s1; const uint64_t *off1;
+    const uint8_t *s2; const uint64_t *off2;
+    const uint32_t *order;        /* pairs sorted by shape */
+    uint64_t n_pairs;
+    uint64_t next_batch;          /* shared work counter   */
+    pthread_mutex_t lock;
+    int32_t *scores;
+    int rc;
+} simd_ctx;
+
+/* One batch of up to PA_LANES pairs, one pair per int16 lane.  Like the
+ * reference's bulk vectors (dp_vector_bulk.hpp:83-103) the lanes are padded to
+ * the longest pair; padding symbols never match and padded cells never feed a
+ * real cell, so only the per-lane result cell needs care. */
+static int simd_batch(simd_ctx *x, const uint32_t *ids, int lanes, uint8_t *qbuf, uint8_t *tbuf,
+                      v16s *hrow, v16s *vgap, size_t cap_n)
+{
+    const pa_oracle_cfg *c = x->cfg;
+    const int local = c->local != 0;
+    uint64_t mmax = 0, nmax = 0, ml[PA_LANES], nl[PA_LANES];
+    for (int l = 0; l < PA_LANES; ++l) {
+        uint32_t k = ids[l < lanes ? l : 0];
+        ml[l] = x->off1[k + 1] - x->off1[k];
+        nl[l] = x->off2[k + 1] - x->off2[k];
+        if (ml[l] > mmax) mmax = ml[l];
+        if (nl[l] > nmax) nmax = nl[l];
+    }
+    if (nmax + 1 > cap_n) return PA_ORACLE_ENOMEM;
+    /* transpose: qbuf[i*L + l], tbuf[j*L + l]; pads 0x00 (query) / 0x01 (target) */
+    for (int l = 0; l < PA_LANES; ++l) {
+        uint32_t k = ids[l < lanes ? l : 0];
+        const uint8_t *a = x->s1 + x->off1[k], *b = x->s2 + x->off2[k];
+        for (uint64_t i = 0; i < mmax; ++i) qbuf[i * PA_LANES + l] = i < ml[l] ? a[i] : 0x00;
+        for (uint64_t j = 0; j < nmax; ++j) tbuf[j * PA_LANES + l] = j < nl[l] ? b[j] : 0x01;
+    }
+    const int16_t goe = (int16_t)(c->gap_open + c->gap_extension), ext = (int16_t)c->gap_extension;
+    const int fcf = local || c->first_column_free, frf = local || c->first_row_free;
+    v16s vgoe, vext, vmatch, vmis, zero, best;
+    for (int l = 0; l < PA_LANES; ++l) {
+        vgoe[l] = goe; vext[l] = ext; vmatch[l] = (int16_t)c->match; vmis[l] = (int16_t)c->mismatch;
+        zero[l] = 0; best[l] = INT16_MIN;
+    }
+    for (uint64_t j = 0; j <= nmax; ++j) {
+        int16_t h = (!frf && j > 0) ? (int16_t)(c->gap_open + c->gap_extension * (int64_t)j) : 0;
+        for (int l = 0; l < PA_LANES; ++l) { hrow[j][l] = h; vgap[j][l] = (int16_t)(h + goe); }
+    }
+    int32_t res[PA_LANES];
+    for (int l = 0; l < PA_LANES; ++l) if (!local && ml[l] == 0) res[l] = hrow[nl[l]][l];
+    for (uint64_t i = 1; i <= mmax; ++i) {
+        int16_t hc = (!fcf) ? (int16_t)(c->gap_open + c->gap_extension * (int64_t)i) : 0;
+        v16s hgap, diag = hrow[0];
+        for (int l = 0; l < PA_LANES; ++l) { hgap[l] = (int16_t)(hc + goe); hrow[0][l] = hc; }
+        v16s qa;
+        for (int l = 0; l < PA_LANES; ++l) qa[l] = qbuf[(i - 1) * PA_LANES + l];
+        for (uint64_t j = 1; j <= nmax; ++j) {
+            v16s tb;
+            for (int l = 0; l < PA_LANES; ++l) tb[l] = tbuf[(j - 1) * PA_LANES + l];
+            v16s d = diag + vsel((v16s)(qa == tb), vmatch, vmis);
+            if (local) d = vmax(d, zero);
+            v16s h = vmax(vmax(d, vgap[j]), hgap);
+            diag = hrow[j];
+            hrow[j] = h;
+            if (local) best = vmax(best, h);
+            v16s hoe = h + vgoe;
+            vgap[j] = vmax(vgap[j] + vext, hoe);
+            hgap = vmax(hgap + vext, hoe);
+        }
+        if (!local)
+            for (int l = 0; l < PA_LANES; ++l) if (ml[l] == i) res[l] = hrow[nl[l]][l];
+    }
+    for (int l = 0; l < lanes; ++l) {
+        if (local) res[l] = (ml[l] == 0 || nl[l] == 0) ? INT32_MIN : best[l];
+        x->scores[ids[l]] = res[l];
+    }
+    return PA_ORACLE_OK;
+}
+
+static void *simd_worker(void *p)
+{
+    simd_ctx *x = (simd_ctx *)p;
+    size_t cap_n = 0;
+    uint8_t *qbuf = NULL, *tbuf = NULL;
+    v16s *hrow = NULL, *vgap = NULL;
+    for (;;) {
+        pthread_mutex_lock(&x->lock);
+        uint64_t b = x->next_batch++;
+        int rc_seen = x->rc;
+        pthread_mutex_unlock(&x->lock);
+        uint64_t first = b * PA_LANES;
+        if (rc_seen || first >= x->n_pairs) break;
+        int lanes = (int)((x->n_pairs - first) < PA_LANES ? (x->n_pairs - first) : PA_LANES);
+        const uint32_t *ids = x->order + first;
+        uint64_t mmax = 0, nmax = 0;
+        for (int l = 0; l < lanes; ++l) {
+            uint64_t m = x->off1[ids[l] + 1] - x->off1[ids[l]], n = x->off2[ids[l] + 1] - x->off2[ids[l]];
+            if (m > mmax) mmax = m;
+            if (n > nmax) nmax = n;
+        }
+        if (nmax + 1 > cap_n || mmax + 1 > cap_n) {
+            cap_n = (nmax > mmax ? nmax : mmax) + 1;
+            free(qbuf); free(tbuf); free(hrow); free(vgap);
+            qbuf = (uint8_t *)malloc(cap_n * PA_LANES);
+            tbuf = (uint8_t *)malloc(cap_n * PA_LANES);
+            hrow = (v16s *)aligned_alloc(32, cap_n * sizeof(v16s));
+            vgap = (v16s *)aligned_alloc(32, cap_n * sizeof(v16s));
+            if (!qbuf || !tbuf || !hrow || !vgap) {
+                pthread_mutex_lock(&x->lock); x->rc = PA_ORACLE_ENOMEM; pthread_mutex_unlock(&x->lock);
+                break;
+            }
+        }
+        int rc = simd_batch(x, ids, lanes, qbuf, tbuf, hrow, vgap, cap_n);
+        if (rc) { pthread_mutex_lock(&x->lock); x->rc = rc; pthread_mutex_unlock(&x->lock); break; }
+    }
+    free(qbuf); free(tbuf); free(hrow); free(vgap);
+    return NULL;
+}
+
+static const uint64_t *g_sort_off1, *g_sort_off2;
+static int cmp_shape(const void *pa, const void *pb)
+{
+    uint32_t a = *(const uint32_t *)pa, b = *(const uint32_t *)pb;
+    uint64_t ma = g_sort_off1[a + 1] - g_sort_off1[a], mb = g_sort_off1[b + 1] - g_sort_off1[b];
+    uint64_t na = g_sort_off2[a + 1] - g_sort_off2[a], nb = g_sort_off2[b + 1] - g_sort_off2[b];
+    if (na != nb) return na < nb ? -1 : 1;
+    if (ma != mb) return ma < mb ? -1 : 1;
+    return a < b ? -1 : (a > b);
+}
+
+/* Worst |value| an int16 lane can see for this pair; mirrors the overflow
+ * guard a caller of the reference's int16 SIMD model must respect. */
+static int fits_int16(const pa_oracle_cfg *c, uint64_t m, uint64_t n)
+{
+    int64_t a = llabs((int64_t)c->match), b = llabs((int64_t)c->mismatch);
+    int64_t o = llabs((int64_t)c->gap_open), e = llabs((int64_t)c->gap_extension);
+    int64_t s = a > b ? a : b;
+    int64_t bound = s * (int64_t)(m < n ? m : n) + 2 * o + e * (int64_t)(m + n + 2) + o + e;
+    return bound < 32000;
+}
+
+int pa_oracle_simd_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint64_t *off1,
+                         const uint8_t *s2, const uint64_t *off2, uint64_t n_pairs,
+                         int32_t *scores, int nthreads)
+{
+    if (!c || !scores || (n_pairs && (!off1 || !off2))) return PA_ORACLE_EINVAL;
+    if (c->local == 0 && (c->last_column_free || c->last_row_free)) return PA_ORACLE_EINVAL;
+    uint32_t *order = (uint32_t *)malloc(sizeof(uint32_t) * (n_pairs ? n_pairs : 1));
+    if (!order) return PA_ORACLE_ENOMEM;
+    uint64_t n_simd = 0;
+    for (uint64_t k = 0; k < n_pairs; ++k) {
+        uint64_t m = off1[k + 1] - off1[k], n = off2[k + 1] - off2[k];
+        if (fits_int16(c, m, n)) order[n_simd++] = (uint32_t)k;
+        else {                                    /* too wide for int16 lanes: scalar int64 */
+            int64_t sc, e1, e2;
+            int rc = pa_oracle_align(c, s1 + off1[k], m, s2 + off2[k], n, &sc, &e1, &e2);
+            if (rc) { free(order); return rc; }
+            scores[k] = (int32_t)sc;
+        }
+    }
+    g_sort_off1 = off1; g_sort_off2 = off2;
+    qsort(order, n_simd, sizeof(uint32_t), cmp_shape);
+    simd_ctx x;
+    memset(&x, 0, sizeof(x));
+    x.cfg = c; x.s1 = s1; x.off1 = off1; x.s2 = s2; x.off2 = off2;
+    x.order = order; x.n_pairs = n_simd; x.scores = scores;
+    pthread_mutex_init(&x.lock, NULL);
+    if (nthreads < 1) nthreads = 1;
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    for (int t = 1; t < nthreads; ++t) pthread_create(&th[t], NULL, simd_worker, &x);
+    simd_worker(&x);
+    for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+    free(th);
+    pthread_mutex_destroy(&x.lock);
+    free(order);
+    return x.rc;
+}

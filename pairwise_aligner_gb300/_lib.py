@@ -1,0 +1,147 @@
+"""ctypes binding of the C ABI in include/pairwise_aligner_gb300.h (libpa_gb300.so).
+
+The shared library is built in-tree by ``pairwise_aligner_gb300.build``.  There is
+no CPU fallback: if the library is missing or no CUDA device is present, the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpa_gb300.so")
+
+PA_METHOD_GLOBAL = 0
+PA_METHOD_LOCAL = 1
+
+STATUS = {
+    0: "PA_OK", 1: "PA_ERR_INVALID_ARGUMENT", 2: "PA_ERR_CUDA", 3: "PA_ERR_OUT_OF_MEMORY",
+    4: "PA_ERR_OVERFLOW", 5: "PA_ERR_UNSUPPORTED", 6: "PA_ERR_TIMEOUT", 7: "PA_ERR_NO_DEVICE",
+    8: "PA_ERR_TOO_LARGE",
+}
+
+RESULT_RERUN, RESULT_BANDED, RESULT_FULL_DP, RESULT_TRIVIAL = 0x01, 0x02, 0x04, 0x08
+
+
+class PaConfig(ctypes.Structure):
+    _fields_ = [
+        ("method", ctypes.c_int32),
+        ("match", ctypes.c_int32),
+        ("mismatch", ctypes.c_int32),
+        ("gap_open", ctypes.c_int32),
+        ("gap_extension", ctypes.c_int32),
+        ("first_column_free", ctypes.c_uint8),
+        ("first_row_free", ctypes.c_uint8),
+        ("last_column_free", ctypes.c_uint8),
+        ("last_row_free", ctypes.c_uint8),
+        ("width_hint", ctypes.c_int32),
+        ("band_mode", ctypes.c_int32),
+    ]
+
+
+class PaResult(ctypes.Structure):
+    _fields_ = [
+        ("score", ctypes.c_int32),
+        ("end1", ctypes.c_int32),
+        ("end2", ctypes.c_int32),
+        ("width", ctypes.c_uint8),
+        ("flags", ctypes.c_uint8),
+        ("band_rounds", ctypes.c_uint16),
+    ]
+
+
+class PaOptions(ctypes.Structure):
+    _fields_ = [
+        ("group_threads", ctypes.c_int32),
+        ("rows_per_thread", ctypes.c_int32),
+        ("blocks_per_sm", ctypes.c_int32),
+        ("use_graphs", ctypes.c_int32),
+        ("autotune", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
+    ]
+
+
+class PaStats(ctypes.Structure):
+    _fields_ = [
+        ("pairs", ctypes.c_uint64),
+        ("cells", ctypes.c_uint64),
+        ("pairs_s16", ctypes.c_uint64),
+        ("pairs_s32", ctypes.c_uint64),
+        ("pairs_general", ctypes.c_uint64),
+        ("pairs_rerun", ctypes.c_uint64),
+        ("pairs_trivial", ctypes.c_uint64),
+        ("kernel_launches", ctypes.c_uint64),
+        ("device_ms", ctypes.c_double),
+        ("dp_ms", ctypes.c_double),
+    ]
+
+
+class PaRoofline(ctypes.Structure):
+    _fields_ = [
+        ("s16x2_cells_per_s", ctypes.c_double),
+        ("s32_cells_per_s", ctypes.c_double),
+        ("sm_clock_mhz", ctypes.c_double),
+        ("sm_count", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+# Every symbol include/pairwise_aligner_gb300.h declares, with its ctypes signature.
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_ctxp = ctypes.c_void_p
+SIGNATURES = {
+    "pa_create": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.POINTER(PaOptions)], ctypes.c_int),
+    "pa_destroy": ([_ctxp], ctypes.c_int),
+    "pa_align_batch": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                        ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(PaStats)], ctypes.c_int),
+    "pa_align_batch_device": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
+                               ctypes.c_void_p, ctypes.POINTER(PaStats)], ctypes.c_int),
+    "pa_align_one_to_many": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(PaStats)],
+                             ctypes.c_int),
+    "pa_measure_roofline": ([_ctxp, ctypes.POINTER(PaRoofline)], ctypes.c_int),
+    "pa_status_string": ([ctypes.c_int], ctypes.c_char_p),
+    "pa_last_error": ([_ctxp], ctypes.c_char_p),
+    "pa_abi_version": ([], ctypes.c_int),
+}
+
+_lib = None
+
+
+class PaError(RuntimeError):
+    """A non-OK pa_status; mirrors the reference's std::runtime_error."""
+
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {message}" if message else STATUS.get(status, str(status)))
+
+
+def load(path: str | None = None):
+    """Load libpa_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError(f"{p} is missing: build it with pairwise_aligner_gb300.build.build() "
+                      "(there is no CPU fallback)")
+    lib = ctypes.CDLL(p)
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(status: int, ctx=None):
+    if status != 0:
+        msg = ""
+        if ctx is not None:
+            raw = load().pa_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        raise PaError(status, msg)

@@ -1,0 +1,207 @@
+"""The aligner object returned by ``cfg.configure_aligner`` and its results.
+
+Mirrors the reference's interface objects:
+  * ``compute(seqs1, seqs2)`` -> list of results, like
+    interface_one_to_one_bulk::compute (interface/interface_one_to_one_bulk.hpp:47-100),
+    without the "<= lane count" limit (:55-57);
+  * ``compute(seq1, seqs2)`` with a single first sequence -> one-to-many
+    (interface/interface_one_to_many_bulk.hpp:47-92);
+  * ``compute(seq1, seq2)`` with two single sequences -> one result
+    (interface/interface_one_to_one_single.hpp:44-67).
+Results expose ``score()``, ``sequence1()``, ``sequence2()`` like
+aligner_result_bulk (result/aligner_result_bulk.hpp:43-69), plus
+``end_position()``.
+
+Bulk callers that hold their sequences as concatenated bytes + offsets use
+``compute_arrays`` (host numpy) or ``compute_device`` (device tensors).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib
+
+
+def pack(seqs: Sequence) -> tuple[np.ndarray, np.ndarray]:
+    """Concatenate str/bytes sequences -> (uint8 bytes, uint64 offsets of length n+1)."""
+    raw = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+    lens = np.fromiter((len(r) for r in raw), dtype=np.uint64, count=len(raw))
+    off = np.zeros(len(raw) + 1, dtype=np.uint64)
+    np.cumsum(lens, out=off[1:])
+    data = np.frombuffer(b"".join(raw), dtype=np.uint8) if raw else np.zeros(0, np.uint8)
+    return data, off
+
+
+class Context:
+    """Owns one pa_ctx (CUDA stream, device buffers, graph cache) on one device."""
+
+    def __init__(self, device: int = 0, group_threads: int = 0, blocks_per_sm: int = 0, use_graphs: int = 0):
+        self.lib = _lib.load()
+        self.ptr = ctypes.c_void_p()
+        opt = _lib.PaOptions()
+        opt.group_threads = group_threads
+        opt.blocks_per_sm = blocks_per_sm
+        opt.use_graphs = use_graphs
+        _lib.check(self.lib.pa_create(ctypes.byref(self.ptr), int(device), ctypes.byref(opt)))
+        self.device = device
+
+    def close(self):
+        if self.ptr:
+            self.lib.pa_destroy(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def roofline(self) -> dict:
+        r = _lib.PaRoofline()
+        _lib.check(self.lib.pa_measure_roofline(self.ptr, ctypes.byref(r)), self.ptr)
+        return {"s16x2_cells_per_s": r.s16x2_cells_per_s, "s32_cells_per_s": r.s32_cells_per_s,
+                "sm_clock_mhz": r.sm_clock_mhz, "sm_count": r.sm_count}
+
+
+RESULT_DTYPE = np.dtype([("score", np.int32), ("end1", np.int32), ("end2", np.int32), ("width", np.uint8),
+                         ("flags", np.uint8), ("band_rounds", np.uint16)])
+assert RESULT_DTYPE.itemsize == ctypes.sizeof(_lib.PaResult)
+
+
+class AlignerResult:
+    """One alignment result (score only, plus the end position)."""
+
+    __slots__ = ("_seq1", "_seq2", "_score", "_end", "_width", "_flags")
+
+    def __init__(self, seq1, seq2, score, end1, end2, width, flags):
+        self._seq1, self._seq2 = seq1, seq2
+        self._score, self._end = int(score), (int(end1), int(end2))
+        self._width, self._flags = int(width), int(flags)
+
+    def score(self) -> int:
+        return self._score
+
+    def sequence1(self):
+        return self._seq1
+
+    def sequence2(self):
+        return self._seq2
+
+    def end_position(self) -> tuple[int, int]:
+        """1-based (end in sequence1, end in sequence2); ties to the smallest first, then second."""
+        return self._end
+
+    def width(self) -> int:
+        return self._width
+
+    def flags(self) -> int:
+        return self._flags
+
+    def __repr__(self):
+        return f"AlignerResult(score={self._score}, end={self._end})"
+
+
+class Aligner:
+    """Configured aligner; see the module docstring."""
+
+    def __init__(self, config: dict, device: int = 0, context: Context | None = None):
+        self.config = dict(config)
+        self.device = device
+        self._ctx = context
+        self.last_stats: dict | None = None
+
+    # -- plumbing -----------------------------------------------------------
+    @property
+    def context(self) -> Context:
+        if self._ctx is None:
+            self._ctx = Context(self.device)
+        return self._ctx
+
+    def c_config(self) -> _lib.PaConfig:
+        c = self.config
+        return _lib.PaConfig(
+            _lib.PA_METHOD_LOCAL if c["local"] else _lib.PA_METHOD_GLOBAL, c["match"], c["mismatch"],
+            c["gap_open"], c["gap_extension"], int(c["first_column_free"]), int(c["first_row_free"]),
+            int(c["last_column_free"]), int(c["last_row_free"]), int(c.get("width_hint", 0)),
+            int(c.get("band_mode", 0)))
+
+    @staticmethod
+    def _stats_dict(st: _lib.PaStats) -> dict:
+        return {name: getattr(st, name) for name, _ in _lib.PaStats._fields_}
+
+    # -- bulk entry points ----------------------------------------------------
+    def compute_arrays(self, seq1: np.ndarray, off1: np.ndarray, seq2: np.ndarray, off2: np.ndarray,
+                       stats: bool = True) -> np.ndarray:
+        """Host arrays in, structured result array (RESULT_DTYPE) out.  Synchronous."""
+        n = len(off1) - 1
+        if len(off2) - 1 != n:
+            raise ValueError("both sequence collections must hold the same number of sequences")
+        seq1 = np.ascontiguousarray(seq1, dtype=np.uint8)
+        seq2 = np.ascontiguousarray(seq2, dtype=np.uint8)
+        off1 = np.ascontiguousarray(off1, dtype=np.uint64)
+        off2 = np.ascontiguousarray(off2, dtype=np.uint64)
+        out = np.zeros(max(n, 1), dtype=RESULT_DTYPE)
+        st = _lib.PaStats()
+        ctx = self.context
+        cfg = self.c_config()
+        rc = ctx.lib.pa_align_batch(ctx.ptr, ctypes.byref(cfg), seq1.ctypes.data, off1.ctypes.data,
+                                    seq2.ctypes.data, off2.ctypes.data, n, out.ctypes.data,
+                                    ctypes.byref(st) if stats else None)
+        _lib.check(rc, ctx.ptr)
+        if stats:
+            self.last_stats = self._stats_dict(st)
+        return out[:n]
+
+    def compute_device(self, seq1, off1, seq2, off2, out, stream=None, stats: bool = False):
+        """Device tensors (torch, uint8 / int64 / a 16-byte-per-pair result buffer) in and out.
+
+        Asynchronous on ``stream`` (a torch.cuda.Stream or raw handle) unless stats=True."""
+        n = off1.numel() - 1
+        st = _lib.PaStats()
+        ctx = self.context
+        cfg = self.c_config()
+        handle = getattr(stream, "cuda_stream", stream)
+        if stream is not None and not handle:
+            handle = 1          # cudaStreamLegacy: torch's default stream
+        handle = handle or None
+        rc = ctx.lib.pa_align_batch_device(ctx.ptr, ctypes.byref(cfg), seq1.data_ptr(), off1.data_ptr(),
+                                           seq1.numel(), seq2.data_ptr(), off2.data_ptr(), seq2.numel(), n,
+                                           out.data_ptr(), handle, ctypes.byref(st) if stats else None)
+        _lib.check(rc, ctx.ptr)
+        if stats:
+            self.last_stats = self._stats_dict(st)
+        return out
+
+    # -- reference-shaped entry point ------------------------------------------
+    def compute(self, seqs1, seqs2):
+        single1 = isinstance(seqs1, (str, bytes, bytearray))
+        single2 = isinstance(seqs2, (str, bytes, bytearray))
+        if single1 and single2:
+            return self.compute([seqs1], [seqs2])[0]
+        if single1:
+            return self._one_to_many(seqs1, list(seqs2))
+        seqs1, seqs2 = list(seqs1), list(seqs2)
+        s1, o1 = pack(seqs1)
+        s2, o2 = pack(seqs2)
+        res = self.compute_arrays(s1, o1, s2, o2)
+        return [AlignerResult(a, b, r["score"], r["end1"], r["end2"], r["width"], r["flags"])
+                for a, b, r in zip(seqs1, seqs2, res)]
+
+    def _one_to_many(self, query, targets):
+        q = query.encode() if isinstance(query, str) else bytes(query)
+        qa = np.frombuffer(q, dtype=np.uint8) if q else np.zeros(1, np.uint8)
+        s2, o2 = pack(targets)
+        n = len(targets)
+        out = np.zeros(max(n, 1), dtype=RESULT_DTYPE)
+        st = _lib.PaStats()
+        ctx = self.context
+        cfg = self.c_config()
+        rc = ctx.lib.pa_align_one_to_many(ctx.ptr, ctypes.byref(cfg), qa.ctypes.data, len(q), s2.ctypes.data,
+                                          o2.ctypes.data, n, out.ctypes.data, ctypes.byref(st))
+        _lib.check(rc, ctx.ptr)
+        self.last_stats = self._stats_dict(st)
+        return [AlignerResult(query, b, r["score"], r["end1"], r["end2"], r["width"], r["flags"])
+                for b, r in zip(targets, out[:n])]

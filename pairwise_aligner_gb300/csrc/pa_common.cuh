@@ -1,0 +1,76 @@
+// pa_common.cuh -- shared device-side types of the GB300 affine-gap DP.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/pairwise_aligner_gb300.h"
+
+namespace pa {
+
+// Score-model parameters, uniform over a launch.  Signs follow the reference:
+// a gap of length k scores gap_open + k * gap_ext (affine_dp_algorithm.hpp:149-155).
+struct DpParams {
+    int32_t match, mismatch, gap_open, gap_ext;
+    int32_t local;
+    int32_t first_column_free, first_row_free, last_column_free, last_row_free;
+    int32_t floor16;      // lower clamp of s16 global lanes
+    int32_t smax;         // max(match, mismatch, 0): best gain of one diagonal step
+    int32_t spad;         // score of a padded cell, <= 0 and <= every real score
+};
+
+// Work classes produced by the classifier; the class is the top field of the bucket key.
+enum Klass : uint32_t { K_S16 = 0, K_S32 = 1, K_GEN = 2, K_NONE = 3 };
+
+constexpr int kKeyBits = 18;                 // 2 class | 6 pass | 10 length bits
+constexpr uint32_t kBuckets = 1u << kKeyBits;
+constexpr int kClassShift = 16;
+
+// Boundary row cell between passes of one group: H and the downward gap of the
+// last held row of a pass, per streamed column (both lanes packed for s16x2).
+struct __align__(8) Cell {
+    uint32_t h, e;
+};
+
+// Per-launch description of a DP class.
+struct DpLaunch {
+    const uint8_t *seq1;          // streamed sequences (raw bytes)
+    const uint64_t *off1;
+    const uint8_t *seq2;          // held sequences (raw bytes)
+    const uint64_t *off2;
+    const uint32_t *qtab;         // per query base 4-byte score table (+1 pad entry per pair)
+    const uint32_t *order;        // pair ids, bucket-sorted
+    const uint32_t *begin_ptr;    // first entry of this class in `order`
+    const uint32_t *count_ptr;    // number of pairs of this class
+    uint32_t *unit_counter;       // persistent-queue head
+    pa_result *out;
+    Cell *boundary;               // pass-boundary scratch: (seq1_bytes + n_pairs) cells
+    uint32_t *rerun_list;         // s16 global results that failed their exactness check
+    uint32_t *rerun_count;
+    unsigned long long *dp_cells; // statistics: cells computed (incl. padding), may be null
+    int32_t G;                    // threads per group (1..32, power of two)
+    int32_t rerun;                // this launch consumes a rerun list
+};
+
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)
+{
+    uint32_t d;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
+    return d;
+}
+
+// 2-bit code of an upper-case DNA byte: A=0 C=1 G=2 T=3; valid iff the byte is one of them.
+__device__ __forceinline__ uint32_t dna_code(uint32_t b) { return ((b >> 1) ^ (b >> 2)) & 3u; }
+__device__ __forceinline__ bool dna_valid(uint32_t b)
+{
+    return ((0x54474341u >> (8u * dna_code(b))) & 0xffu) == b;
+}
+
+// Border cell of the first row / column (affine_initialisation_strategy.hpp:38-51):
+// index 0 -> 0, penalised index k -> open + ext * k, free -> 0.  The matching gap
+// value is border + (open + ext).
+__device__ __forceinline__ int32_t border(const DpParams &p, int free_rule, int64_t k)
+{
+    return (free_rule || k == 0) ? 0 : (int32_t)(p.gap_open + (int64_t)p.gap_ext * k);
+}
+
+}  // namespace pa

@@ -1,0 +1,200 @@
+// pa_prep.cuh -- batch preparation on the device: classify, encode, bucket.
+//
+// Replaces the reference's per-batch transposition and padding into SIMD lanes
+// (include/pairwise_aligner/matrix/dp_vector_bulk.hpp:83-103): here every pair
+// keeps its own length; pairs are only grouped so that the lanes and groups of
+// one warp get matrices of nearly the same shape.
+#pragma once
+#include "pa_common.cuh"
+
+namespace pa {
+
+struct ClassCfg {
+    int32_t fast_scores;     // match/mismatch fit a signed byte table
+    int32_t s16_params;      // gap scores small enough for s16 lanes
+    int32_t force32;         // width hint 32
+    int32_t local;
+    int32_t rows[3];         // rows per pass (G*R) of each DP class
+    int32_t gcnt[3];         // G of each class (for the last-pass chunk count)
+    int32_t rpt[3];          // R of each class
+};
+
+struct PrepStats {
+    unsigned long long cells;
+    unsigned long long n_class[4];
+    unsigned long long overflow;    // pairs whose int32 bound fails
+};
+
+__device__ __forceinline__ uint32_t quant_len(uint32_t m)
+{
+    if (m < 32u) return m;
+    const uint32_t e = 31u - __clz(m);
+    return min(1023u, 32u + (e - 5u) * 32u + ((m >> (e - 5u)) & 31u));
+}
+
+__device__ __forceinline__ uint32_t quant_shape(uint32_t s)
+{
+    if (s < 32u) return s;
+    const uint32_t e = 31u - __clz(s);
+    return min(63u, 32u + (e - 5u) * 4u + ((s >> (e - 2u)) & 3u));
+}
+
+// 4-byte score table of a streamed base: match in byte code(b), mismatch elsewhere;
+// a byte outside A/C/G/T matches nothing.
+__device__ __forceinline__ uint32_t score_table(uint32_t b, uint32_t match4, uint32_t mis4)
+{
+    if (!dna_valid(b)) return mis4;
+    return prmt(match4, mis4, 0x4444u ^ (4u << (4u * dna_code(b))));
+}
+
+// Result of a pair with an empty sequence (no DP needed); same candidate rules as the DP.
+__device__ void trivial_result(const DpParams &P, int32_t m, int32_t n, pa_result &r)
+{
+    r.width = 32;
+    r.flags = PA_RESULT_TRIVIAL;
+    r.band_rounds = 0;
+    if (P.local) { r.score = INT32_MIN; r.end1 = 0; r.end2 = 0; return; }
+    int32_t s, i, j;
+    if (m == 0) { s = border(P, P.first_row_free, n); i = 0; j = n; }
+    else { s = border(P, P.first_column_free, m); i = m; j = 0; }
+    auto take = [&](int32_t x, int32_t xi, int32_t xj) {
+        if (x > s || (x == s && (xi < i || (xi == i && xj < j)))) { s = x; i = xi; j = xj; }
+    };
+    if (m == 0 && P.last_row_free) take(0, 0, 0);        // H(0, 0..n): the maximum is H(0,0)
+    if (n == 0 && P.last_column_free) take(0, 0, 0);     // H(0..m, 0): likewise
+    r.score = s; r.end1 = i; r.end2 = j;
+}
+
+// One warp per pair: check sequence2's alphabet, pick the class, write the bucket
+// key, the score tables of sequence1 and the trivial results.
+__global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__restrict__ off1,
+                           const uint8_t *__restrict__ seq2, const uint64_t *__restrict__ off2,
+                           uint64_t n_pairs, DpParams P, ClassCfg C, uint32_t *__restrict__ keys,
+                           uint32_t *__restrict__ hist, uint32_t *__restrict__ qtab, pa_result *__restrict__ out,
+                           PrepStats *__restrict__ st)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t match4 = (uint8_t)P.match * 0x01010101u;
+    const uint32_t mis4 = (uint8_t)P.mismatch * 0x01010101u;
+    for (uint64_t p = warp; p < n_pairs; p += nwarps) {
+        const uint64_t q0 = off1[p], t0 = off2[p];
+        const int64_t m = (int64_t)(off1[p + 1] - q0), n = (int64_t)(off2[p + 1] - t0);
+        bool dna = true;
+        for (int64_t j = lane; j < n; j += 32) dna &= dna_valid(seq2[t0 + j]);
+        dna = __all_sync(0xffffffffu, dna);
+        uint32_t klass;
+        if (m == 0 || n == 0) klass = K_NONE;
+        else if (!C.fast_scores || !dna) klass = K_GEN;
+        else if (!C.force32 && C.s16_params && (int64_t)P.smax * min(m, n) <= 30000) klass = K_S16;
+        else klass = K_S32;
+        if (klass == K_S16 || klass == K_S32) {
+            uint32_t *qt = qtab + q0 + p;
+            for (int64_t i = lane; i <= m; i += 32)
+                qt[i] = (i < m) ? score_table(seq1[q0 + i], match4, mis4) : 0x80808080u;
+        }
+        if (lane == 0) {
+            const int64_t a = P.match < 0 ? -(int64_t)P.match : P.match;
+            const int64_t b = P.mismatch < 0 ? -(int64_t)P.mismatch : P.mismatch;
+            const int64_t o = -(int64_t)P.gap_open, e = -(int64_t)P.gap_ext;
+            const int64_t bound = (a + b) * min(m, n) + (o + e) * (m + n + 2) + 2 * o;
+            if (bound >= (1ll << 30)) atomicAdd(&st->overflow, 1ull);
+            uint32_t key;
+            if (klass == K_NONE) {
+                pa_result r;
+                trivial_result(P, (int32_t)m, (int32_t)n, r);
+                out[p] = r;
+                key = (uint32_t)K_NONE << kClassShift;
+            } else {
+                const int32_t rows = C.rows[klass], G = C.gcnt[klass], R = C.rpt[klass];
+                const int64_t passes = (n + rows - 1) / rows;
+                const int64_t rem = n - (passes - 1) * rows;
+                const int64_t nch = (rem + G * 4 - 1) / (G * 4);
+                const uint64_t shape = (uint64_t)(passes - 1) * (R / 4) + (uint64_t)(nch - 1);
+                key = (klass << kClassShift) | (quant_shape(shape > 0xffffffffull ? 0xffffffffu : (uint32_t)shape) << 10) |
+                      quant_len((uint32_t)m);
+                atomicAdd(&st->cells, (unsigned long long)(m * n));
+            }
+            keys[p] = key;
+            atomicAdd(&hist[key], 1u);
+            atomicAdd(&st->n_class[klass], 1ull);
+        }
+    }
+}
+
+// Exclusive scan of kBuckets counters in three kernels (1024 counters per block).
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *sh, uint32_t &total)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        sh[lane] = s;
+    }
+    __syncthreads();
+    total = sh[(blockDim.x >> 5) - 1];
+    const uint32_t before = (w > 0) ? sh[w - 1] : 0u;
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void k_scan_blocks(const uint32_t *__restrict__ hist, uint32_t *__restrict__ starts,
+                              uint32_t *__restrict__ sums)
+{
+    __shared__ uint32_t sh[32];
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t total;
+    const uint32_t ex = block_exclusive_scan(hist[x], sh, total);
+    starts[x] = ex;
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_sums(uint32_t *__restrict__ sums, uint32_t nblocks)
+{
+    __shared__ uint32_t sh[32];
+    uint32_t total;
+    const uint32_t v = threadIdx.x < nblocks ? sums[threadIdx.x] : 0u;
+    const uint32_t ex = block_exclusive_scan(v, sh, total);
+    if (threadIdx.x < nblocks) sums[threadIdx.x] = ex;
+}
+
+__global__ void k_scan_add(uint32_t *__restrict__ starts, uint32_t *__restrict__ cursor,
+                           const uint32_t *__restrict__ sums, uint32_t *__restrict__ ranges)
+{
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = starts[x] + sums[blockIdx.x];
+    starts[x] = s;
+    cursor[x] = s;
+    if ((x & ((1u << kClassShift) - 1u)) == 0u) ranges[x >> kClassShift] = s;   // class begin
+}
+
+__global__ void k_scatter(const uint32_t *__restrict__ keys, uint64_t n_pairs, uint32_t *__restrict__ cursor,
+                          uint32_t *__restrict__ order, const uint32_t *__restrict__ ranges,
+                          uint32_t *__restrict__ counts)
+{
+    const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (p == 0) {
+        // class sizes from the class begins (ranges[4] = number of non-trivial pairs)
+        for (int c = 0; c < 3; ++c) counts[c] = ranges[c + 1] - ranges[c];
+    }
+    if (p >= n_pairs) return;
+    const uint32_t key = keys[p];
+    if ((key >> kClassShift) == K_NONE) return;
+    const uint32_t pos = atomicAdd(&cursor[key], 1u);
+    order[pos] = (uint32_t)p;
+}
+
+}  // namespace pa

@@ -1,0 +1,90 @@
+"""The oracle against the reference's own golden vectors (CPU only).
+
+* every hand-written expected score of the reference's scalar tests
+  (test/unit/affine/*_scalar_test.cpp, test/unit/configuration/*.cpp);
+* the reference's differential SIMD-vs-scalar cases: the oracle's
+  inter-sequence SIMD port must agree with its scalar restatement on the exact
+  mt19937(42) pairs the reference's tests align, as the reference's
+  SIMD lanes agree with its scalar aligner (alignment_simd_test_template.hpp:195-227);
+* local end coordinates follow the documented tie-break.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import oracle_cfg_of
+
+
+def test_scalar_kats(oracle, kats):
+    assert len(kats) >= 22
+    for c in kats:
+        sc, e1, e2 = oracle.align(oracle_cfg_of(oracle, c), c["seq1"].encode(), c["seq2"].encode())
+        assert sc == c["expected_score"], (c["source"], c["name"])
+
+
+def test_fixture_scores_are_the_oracles(oracle, simd_cases):
+    # the committed expected values are reproducible from the committed sequences
+    for c in simd_cases[::7]:
+        cfg = oracle_cfg_of(oracle, c)
+        for a, b, s, e1, e2 in list(zip(c["seqs1"], c["seqs2"], c["oracle_scores"], c["oracle_end1"],
+                                        c["oracle_end2"]))[:8]:
+            assert oracle.align(cfg, a.encode(), b.encode()) == (s, e1, e2)
+
+
+def test_simd_port_matches_scalar_on_reference_cases(oracle, simd_cases):
+    from pairwise_aligner_gb300.aligner import pack
+    checked = 0
+    for c in simd_cases:
+        if c["method"] == "global" and (c["last_column"] == "free" or c["last_row"] == "free"):
+            continue                    # the SIMD port times the penalised-trailing / local paths only
+        cfg = oracle_cfg_of(oracle, c)
+        s1, o1 = pack(c["seqs1"])
+        s2, o2 = pack(c["seqs2"])
+        got = oracle.simd_batch(cfg, s1, o1, s2, o2, nthreads=2)
+        assert list(got) == c["oracle_scores"], c["name"]
+        checked += 1
+    assert checked >= 30
+
+
+def test_batch_matches_single(oracle, simd_cases):
+    from pairwise_aligner_gb300.aligner import pack
+    c = simd_cases[3]
+    cfg = oracle_cfg_of(oracle, c)
+    s1, o1 = pack(c["seqs1"])
+    s2, o2 = pack(c["seqs2"])
+    sc, e1, e2 = oracle.align_batch(cfg, s1, o1, s2, o2, nthreads=3)
+    assert list(sc) == c["oracle_scores"]
+    assert list(e1) == c["oracle_end1"] and list(e2) == c["oracle_end2"]
+
+
+def test_local_end_tie_break(oracle):
+    cfg = oracle.make_cfg(1, -1, -2, -1, local=True)
+    # two equal maximal cells: (2,2) and (4,2) / (2,4) ... the smallest i wins, then the smallest j
+    assert oracle.align(cfg, b"AAXAA", b"AA") == (2, 2, 2)
+    assert oracle.align(cfg, b"AA", b"AAXAA") == (2, 2, 2)
+    assert oracle.align(cfg, b"C", b"G") == (0, 0, 0)          # score 0 -> (0, 0)
+    assert oracle.align(cfg, b"", b"G") == (-2**31, 0, 0)      # empty -> lowest(), (0, 0)
+
+
+def test_global_free_end_coordinates(oracle):
+    # overlap: best cell may end inside the last row / column
+    cfg = oracle.make_cfg(4, -5, -10, -1, first_column_free=True, first_row_free=True, last_column_free=True,
+                          last_row_free=True)
+    sc, e1, e2 = oracle.align(cfg, b"TTTTTCTGACACACT", b"CTGCACACGACGGGGGG")
+    assert sc == 16
+    assert 0 <= e1 <= 15 and 0 <= e2 <= 17 and (e1 == 15 or e2 == 17)
+    std = oracle.make_cfg(4, -5, -10, -1)
+    assert oracle.align(std, b"ACGT", b"ACGT") == (16, 4, 4)
+    assert oracle.align(std, b"", b"ACG") == (-13, 0, 3)        # H(0, n) = open + 3 * ext
+    assert oracle.align(std, b"ACG", b"") == (-13, 3, 0)
+
+
+@pytest.mark.parametrize("local", [False, True])
+def test_oracle_symmetry(oracle, local):
+    rng = np.random.default_rng(7)
+    cfg = oracle.make_cfg(2, -3, -5, -1, local=local)
+    for _ in range(20):
+        a = rng.choice(list(b"ACGT"), size=int(rng.integers(1, 40))).astype(np.uint8).tobytes()
+        b = rng.choice(list(b"ACGT"), size=int(rng.integers(1, 40))).astype(np.uint8).tobytes()
+        assert oracle.align(cfg, a, b)[0] == oracle.align(cfg, b, a)[0]
