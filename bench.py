@@ -1,0 +1,324 @@
+#!/usr/bin/env python3
+"""Throughput of the affine-gap score DP on GB300, in GCUPS (full m*n cells per second).
+
+Workload: the local (Smith-Waterman-Gotoh) batch of 262,144 DNA pairs with
+independent lengths uniform in 64..512, half related (15/2/2% mutations) and
+half unrelated, scores +1/-4, gap_model_affine(-6, -1), score plus end
+coordinates.  Synthetic and seeded (pairwise_aligner_gb300.workloads.config2).
+
+One step = one call of the hot path over the whole batch:
+  value  -- inputs already resident in HBM, pa_align_batch_device on one stream,
+            CUDA events around K steps (inputs of ~150 MB plus ~300 MB of score
+            tables exceed the 129 MB L2, so no flush is needed between steps);
+  e2e    -- the same batch through pa_align_batch with pinned HOST buffers:
+            host->device copies, the DP and the device->host result read per step.
+  roofline -- the DP kernels' own duration (events inside the library) against
+            the measured whole-chip rate of the cell-update instruction mix
+            (pa_measure_roofline); HBM traffic against MEASURED_PEAKS.json.
+  cpu_baseline -- the oracle's inter-sequence SIMD port on all host cores, on a
+            bounded sample of the batch (rank 0 only).
+
+--impl reference times the CPU implementation of the path (the reference's own
+build when present, else the oracle's SIMD port) on the host cores.
+N > 1 GPUs (torchrun): independent replicas, one full batch per rank, no
+collective on the data path; value = all ranks' cells / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "GCUPS (m*n cells/s), affine-gap local score DP + end coordinates, bit-exact"
+WORKLOAD = "config2_local_262144_pairs_64-512bp_+1/-4/-6/-1"
+# DRAM bytes per cell of the s16x2 local DP kernel, from the ncu capture summarised in
+# profiles/dp_kernel_s16x2_local_config2.md (dram__bytes_read.sum + dram__bytes_write.sum
+# of a 32,768-pair launch divided by its 2.71e9 cells; traffic grows with the cells).
+DRAM_BYTES_PER_CELL = (49.886976e6 + 4.359168e6) / 2714564472
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_workload(pairs: int | None):
+    from pairwise_aligner_gb300 import workloads as W
+    d = W.config2() if not pairs else W.config2(n_pairs=pairs)
+    return d, W.cells(d)
+
+
+def cpu_sample_rate(d, budget_s: float, threads: int):
+    """Time the oracle's SIMD port on a leading sample of the batch sized to ~budget_s seconds."""
+    import numpy as np
+    from oracle import oracle as O
+    from pairwise_aligner_gb300 import workloads as W
+    cfg = O.make_cfg(d["match"], d["mismatch"], d["gap_open"], d["gap_extension"], local=d["local"])
+    n_total = len(d["off1"]) - 1
+    n = min(n_total, 2048)
+    while True:
+        sub = W.subset(d, np.arange(n))
+        t0 = time.perf_counter()
+        O.simd_batch(cfg, sub["seq1"], sub["off1"], sub["seq2"], sub["off2"], nthreads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= budget_s * 0.5 or n >= n_total:
+            return W.cells(sub) / dt / 1e9, n, dt
+        n = min(n_total, int(n * max(2.0, budget_s / max(dt, 1e-3))))
+
+
+def reference_arm(args):
+    import numpy as np
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    from pairwise_aligner_gb300 import workloads as W
+    d, _ = load_workload(args.pairs)
+    threads = os.cpu_count() or 1
+    kind, label = "port", "oracle inter-sequence int16 SIMD port (oracle/pa_oracle.c), pthreads"
+    ref_lib = os.path.join(REPO, "oracle", "_ref", "libpa_ref.so")
+    if os.path.exists(ref_lib):
+        kind, label = "reference", "reference headers built by oracle/ref_build.py"
+    # one step = a bounded leading sample, sized so W + K steps take about two minutes
+    per_step = max(0.5, min(5.0, 100.0 / max(1, args.steps + args.warmup)))
+    rate, n, dt = cpu_sample_rate(d, per_step, threads)
+    sub = W.subset(d, np.arange(n))
+    cfg = O.make_cfg(d["match"], d["mismatch"], d["gap_open"], d["gap_extension"], local=d["local"])
+    for _ in range(args.warmup):
+        O.simd_batch(cfg, sub["seq1"], sub["off1"], sub["seq2"], sub["off2"], nthreads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.simd_batch(cfg, sub["seq1"], sub["off1"], sub["seq2"], sub["off2"], nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    cells = W.cells(sub)
+    value = cells * len(times) / sum(times) / 1e9
+    sample = f"first {n} of {len(d['off1']) - 1} pairs ({cells:.3g} cells) per step; {label}"
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GCUPS", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16 lanes",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "pairs_per_step": n},
+            "cpu_baseline": {"value": round(value, 3), "unit": "GCUPS", "cores": threads, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def our_arm(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    import pairwise_aligner_gb300 as pa
+    from pairwise_aligner_gb300.aligner import Aligner
+    from pairwise_aligner_gb300 import build as B
+
+    rank, world, local_rank = env_rank()
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group("gloo")
+    B.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    d, cells = load_workload(args.pairs)
+    n = len(d["off1"]) - 1
+    conf = dict(local=d["local"], match=d["match"], mismatch=d["mismatch"], gap_open=d["gap_open"],
+                gap_extension=d["gap_extension"], first_column_free=True, first_row_free=True,
+                last_column_free=True, last_row_free=True, width_hint=0, band_mode=0)
+    ctx = pa.Context(local_rank, group_threads=args.group_threads, kernel_variant=args.variant)
+    al = Aligner(conf, device=local_rank, context=ctx)
+    peak = ctx.roofline()
+
+    s1 = torch.from_numpy(d["seq1"]).to(dev)
+    s2 = torch.from_numpy(d["seq2"]).to(dev)
+    o1 = torch.from_numpy(d["off1"].astype(np.int64)).to(dev)
+    o2 = torch.from_numpy(d["off2"].astype(np.int64)).to(dev)
+    out = torch.empty(n * 16, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    # warm-up (captures the CUDA graph), then K timed steps
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            al.compute_device(s1, o1, s2, o2, out, stream=stream)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        time.sleep(0.3)
+        e0.record(stream)
+        for _ in range(args.steps):
+            al.compute_device(s1, o1, s2, o2, out, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = cells * world / (ms * 1e-3) / 1e9
+
+    # DP kernels alone (events inside the library, same stream), one call at a time
+    dp = []
+    for _ in range(max(3, min(args.steps, 5))):
+        al.compute_device(s1, o1, s2, o2, out, stream=stream, stats=True)
+        dp.append(al.last_stats["dp_ms"])
+    st = al.last_stats
+    dp_ms = statistics.mean(dp)
+    launches_per_step = int(st["kernel_launches"])
+    res = np.frombuffer(out.cpu().numpy().tobytes(), dtype=pa.RESULT_DTYPE)
+
+    # end to end through the host-buffer C ABI from pinned memory
+    pin = {k: torch.from_numpy(np.ascontiguousarray(d[k])).pin_memory() for k in ("seq1", "off1", "seq2", "off2")}
+    hs = {k: v.numpy() for k, v in pin.items()}
+    for _ in range(2):
+        al.compute_arrays(hs["seq1"], hs["off1"], hs["seq2"], hs["off2"], stats=False)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_res = al.compute_arrays(hs["seq1"], hs["off1"], hs["seq2"], hs["off2"], stats=False)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    assert np.array_equal(host_res["score"], res["score"]), "host and device entry points disagree"
+    h2d = int(sum(pin[k].numel() * pin[k].element_size() for k in pin))
+    d2h = n * 16
+
+    achieved = cells / (dp_ms * 1e-3) / 1e9
+    peak_gcups = peak["s16x2_cells_per_s"] / 1e9
+    alg_bytes = int(d["off1"][-1] + d["off2"][-1]) + 16 * n          # inputs read + results written
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int16x2 lanes (int32 where a pair needs it)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "pairs": n, "cells": cells, "group_threads": ctx_G(args),
+                   "l2": "inputs (~150 MB bytes + ~300 MB score tables) larger than the 129 MB L2; no flush",
+                   "pairs_s16": st["pairs_s16"], "pairs_s32": st["pairs_s32"], "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(cells / e2e_s / 1e9 * world, 2), "unit": "GCUPS", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "int_dpx", "achieved": round(achieved, 1), "peak": round(peak_gcups, 1),
+                     "unit": "GCUPS", "frac": round(achieved / peak_gcups, 4),
+                     "traffic": int(DRAM_BYTES_PER_CELL * cells),
+                     "peak_source": "pa_measure_roofline: whole-chip s16x2 cell-update instruction mix, measured live",
+                     "kernel": "dp_kernel<L16> (all DP kernels of one call)", "kernel_ms": round(dp_ms, 4),
+                     "hbm": {"achieved": round(alg_bytes / (dp_ms * 1e-3) / 1e9, 1),
+                             "peak": hbm_peak(), "unit": "GB/s",
+                             "frac": round(alg_bytes / (dp_ms * 1e-3) / 1e9 / hbm_peak(), 5)}},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, npairs, dt = cpu_sample_rate(d, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": round(rate, 3), "unit": "GCUPS", "cores": threads, "kind": "port",
+                                "sample": f"first {npairs} pairs of the batch, {dt:.1f} s, oracle int16 SIMD port"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def hbm_peak() -> float:
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0          # fallback figure of the profiling recipe
+
+
+def ctx_G(args):
+    return args.group_threads or 8
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--pairs", type=int, default=0, help="override the batch size (default: 262,144)")
+    ap.add_argument("--group-threads", type=int, default=0)
+    ap.add_argument("--variant", type=int, default=-1)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    return reference_arm(args) if args.impl == "reference" else our_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -58,7 +58,8 @@ class PaOptions(ctypes.Structure):
         ("blocks_per_sm", ctypes.c_int32),
         ("use_graphs", ctypes.c_int32),
         ("autotune", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 3),
+        ("kernel_variant", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
 

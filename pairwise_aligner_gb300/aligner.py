@@ -38,13 +38,15 @@ def pack(seqs: Sequence) -> tuple[np.ndarray, np.ndarray]:
 class Context:
     """Owns one pa_ctx (CUDA stream, device buffers, graph cache) on one device."""
 
-    def __init__(self, device: int = 0, group_threads: int = 0, blocks_per_sm: int = 0, use_graphs: int = 0):
+    def __init__(self, device: int = 0, group_threads: int = 0, blocks_per_sm: int = 0, use_graphs: int = 0,
+                 kernel_variant: int = -1):
         self.lib = _lib.load()
         self.ptr = ctypes.c_void_p()
         opt = _lib.PaOptions()
         opt.group_threads = group_threads
         opt.blocks_per_sm = blocks_per_sm
         opt.use_graphs = use_graphs
+        opt.kernel_variant = kernel_variant
         _lib.check(self.lib.pa_create(ctypes.byref(self.ptr), int(device), ctypes.byref(opt)))
         self.device = device
 

@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libpa_gb300.so")
-SOURCES = ["pa_capi.cu"]
+SOURCES = ["pa_capi.cu", "pa_kern_v0.cu", "pa_kern_v1.cu", "pa_kern_v2.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -31,17 +31,30 @@ def _stale(target: str) -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile csrc/*.cu into pairwise_aligner_gb300/libpa_gb300.so (skipped when up to date)."""
+    """Compile csrc/*.cu (in parallel) and link pairwise_aligner_gb300/libpa_gb300.so; skipped when up to date."""
     if not force and not _stale(LIB):
         return LIB
-    tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-           "-diag-suppress", "177", "-o", tmp] + [os.path.join(CSRC, s) for s in SOURCES]
+    objdir = os.path.join(HERE, "_build")
+    os.makedirs(objdir, exist_ok=True)
+    flags = [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-        print(" ".join(cmd), file=sys.stderr)
-    subprocess.check_call(cmd)
+        flags.append("-Xptxas=-v")
+    procs, objs = [], []
+    for src in SOURCES:
+        obj = os.path.join(objdir, src.replace(".cu", f".{os.getpid()}.o"))
+        objs.append(obj)
+        cmd = [nvcc(), *flags, "-c", os.path.join(CSRC, src), "-o", obj]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append(subprocess.Popen(cmd))
+    failed = [p.args for p in procs if p.wait() != 0]
+    if failed:
+        raise RuntimeError(f"nvcc failed: {failed}")
+    tmp = LIB + f".tmp{os.getpid()}"
+    subprocess.check_call([nvcc(), *ARCH, "-shared", "-o", tmp, *objs])
     os.replace(tmp, LIB)
+    for o in objs:
+        os.remove(o)
     return LIB
 
 

@@ -23,12 +23,13 @@
 #include "pa_common.cuh"
 #include "pa_dp.cuh"
 #include "pa_prep.cuh"
+#include "pa_launch.h"
 
 using namespace pa;
 
 namespace {
 
-constexpr int kBlock = 256;
+
 constexpr int kR = 16;             // rows per thread per lane
 constexpr int kDefaultG = 8;       // threads per group
 
@@ -51,12 +52,14 @@ struct pa_ctx {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    cudaEvent_t ev_dp0 = nullptr, ev_dp1 = nullptr;   // bracket the DP kernels of the last call
     pa_options opt{};
     std::string err;
     // device work buffers (grow only)
     DevBuf keys, order, hist, starts, cursor, sums, ranges, counts, qtab, boundary, rerun, counters, pstats;
     DevBuf in_seq1, in_off1, in_seq2, in_off2, in_out;   // staging for the host-buffer entry points
     int G[3] = {kDefaultG, kDefaultG, kDefaultG};
+    int variant[3] = {0, 0, 0};
     int grid[3] = {0, 0, 0};
     std::map<GraphKey, cudaGraphExec_t> graphs;
     uint64_t last_launches = 0;
@@ -135,43 +138,53 @@ pa_status check_config(pa_ctx *c, const pa_config *cfg, DpParams &P, ClassCfg &C
     return PA_OK;
 }
 
-// Resident blocks per SM of a DP kernel; queried once (outside any stream capture).
-template <class V, int MODE, bool GEN>
-int occupancy()
+}  // namespace
+
+namespace pa {
+int dp_occupancy_v0(bool lanes16, bool gen, int mode);
+int dp_occupancy_v1(bool lanes16, bool gen, int mode);
+int dp_occupancy_v2(bool lanes16, bool gen, int mode);
+void dp_launch_v0(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
+void dp_launch_v1(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
+void dp_launch_v2(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
+
+int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
 {
-    static int per_sm = -1;
-    if (per_sm < 0) {
-        int v = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel<V, kR, MODE, GEN>, kBlock, 0);
-        per_sm = v < 1 ? 1 : v;
-    }
-    return per_sm;
+    if (variant == 1) return dp_occupancy_v1(lanes16, gen, mode);
+    if (variant == 2) return dp_occupancy_v2(lanes16, gen, mode);
+    return dp_occupancy_v0(lanes16, gen, mode);
 }
 
+void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStream_t st, const DpLaunch &L,
+               const DpParams &P)
+{
+    if (variant == 1) dp_launch_v1(lanes16, gen, mode, grid, st, L, P);
+    else if (variant == 2) dp_launch_v2(lanes16, gen, mode, grid, st, L, P);
+    else dp_launch_v0(lanes16, gen, mode, grid, st, L, P);
+}
+}  // namespace pa
+
+namespace {
+
+// Resident blocks per SM of every DP kernel, queried once outside any stream capture.
 void warm_occupancy()
 {
-    occupancy<L16, M_LOCAL, false>(); occupancy<L16, M_GLOBAL, false>(); occupancy<L16, M_GLOBAL_FREE, false>();
-    occupancy<L32, M_LOCAL, false>(); occupancy<L32, M_GLOBAL, false>(); occupancy<L32, M_GLOBAL_FREE, false>();
-    occupancy<L32, M_LOCAL, true>(); occupancy<L32, M_GLOBAL, true>(); occupancy<L32, M_GLOBAL_FREE, true>();
+    for (int v = 0; v < 3; ++v)
+        for (int mode = 0; mode < 3; ++mode) {
+            dp_occupancy(v, true, false, mode);
+            dp_occupancy(v, false, false, mode);
+            dp_occupancy(v, false, true, mode);
+        }
 }
 
-template <class V, int MODE, bool GEN>
-void launch_dp(pa_ctx *c, int slot, const DpLaunch &L, const DpParams &P)
+void launch_class(pa_ctx *c, int slot, int mode, bool lanes16, bool gen, const DpLaunch &L, const DpParams &P)
 {
-    auto kern = dp_kernel<V, kR, MODE, GEN>;
-    int per_sm = occupancy<V, MODE, GEN>();
+    const int v = c->variant[slot];
+    int per_sm = dp_occupancy(v, lanes16, gen, mode);
     if (c->opt.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)c->opt.blocks_per_sm);
     c->grid[slot] = per_sm * c->sm_count;
-    kern<<<c->grid[slot], kBlock, 0, c->stream>>>(L, P);
+    dp_launch(v, lanes16, gen, mode, c->grid[slot], c->stream, L, P);
     c->last_launches++;
-}
-
-template <class V, bool GEN>
-void launch_mode(pa_ctx *c, int slot, int mode, const DpLaunch &L, const DpParams &P)
-{
-    if (mode == M_LOCAL) launch_dp<V, M_LOCAL, GEN>(c, slot, L, P);
-    else if (mode == M_GLOBAL) launch_dp<V, M_GLOBAL, GEN>(c, slot, L, P);
-    else launch_dp<V, M_GLOBAL_FREE, GEN>(c, slot, L, P);
 }
 
 // Everything between inputs-on-device and results-on-device; no host sync.
@@ -214,15 +227,16 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
 
     const uint32_t *ranges = (const uint32_t *)c->ranges.p;
     const uint32_t *counts = (const uint32_t *)c->counts.p;
+    PA_CUDA(c, cudaEventRecordWithFlags(c->ev_dp0, st, cudaEventRecordExternal));
     // s16x2 class
     L.begin_ptr = ranges + K_S16; L.count_ptr = counts + K_S16; L.unit_counter = counters + 0; L.G = c->G[K_S16];
-    launch_mode<L16, false>(c, K_S16, mode, L, P);
+    launch_class(c, K_S16, mode, true, false, L, P);
     // s32 class
     L.begin_ptr = ranges + K_S32; L.count_ptr = counts + K_S32; L.unit_counter = counters + 1; L.G = c->G[K_S32];
-    launch_mode<L32, false>(c, K_S32, mode, L, P);
+    launch_class(c, K_S32, mode, false, false, L, P);
     // byte-compare class
     L.begin_ptr = ranges + K_GEN; L.count_ptr = counts + K_GEN; L.unit_counter = counters + 2; L.G = c->G[K_GEN];
-    launch_mode<L32, true>(c, K_GEN, mode, L, P);
+    launch_class(c, K_GEN, mode, false, true, L, P);
     // s16 global results that failed the exactness check, recomputed in s32
     if (mode != M_LOCAL) {
         L.order = (const uint32_t *)c->rerun.p;
@@ -231,8 +245,9 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
         L.unit_counter = counters + 3;
         L.rerun = 1;
         L.G = c->G[K_S32];
-        launch_mode<L32, false>(c, K_S32, mode, L, P);
+        launch_class(c, K_S32, mode, false, false, L, P);
     }
+    PA_CUDA(c, cudaEventRecordWithFlags(c->ev_dp1, st, cudaEventRecordExternal));
     PA_CUDA(c, cudaGetLastError());
     (void)cfg;
     return PA_OK;
@@ -316,6 +331,8 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
             float ms = 0.f;
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
             stats->device_ms = ms;
+            if (cudaEventElapsedTime(&ms, c->ev_dp0, c->ev_dp1) == cudaSuccess) stats->dp_ms = ms;
+            cudaGetLastError();
             stats->cells = ps.cells;
             stats->pairs_s16 = ps.n_class[K_S16] - ctr[4];
             stats->pairs_s32 = ps.n_class[K_S32] + ctr[4];
@@ -338,26 +355,26 @@ __global__ void __launch_bounds__(256) k_roofline(int steps, uint32_t seed, uint
 {
     constexpr int R = 16;
     uint32_t H[R], Fr[R], Sel[R];
-    const uint32_t GOE = V::splat(-7), EXT = V::splat(-1), FLOOR = V::splat(-30000);
+    const uint32_t GOEA = V::cabs(-7), EXTA = V::cabs(-1), CLAMP = V::splat(2048);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        H[k] = V::splat((int)((seed + k * 7 + threadIdx.x) & 15));
-        Fr[k] = V::splat(-3);
+        H[k] = V::splat(2048 + (int)((seed + k * 7 + threadIdx.x) & 15));
+        Fr[k] = V::splat(2040);
         Sel[k] = V::selector((k + threadIdx.x) & 3, (k * 3 + threadIdx.x) & 3);
     }
-    uint32_t ta = 0x01fcfcfcu ^ (seed & 0x03000000u), tb = 0xfc01fcfcu, up = 0, diag0 = 0;
+    uint32_t ta = 0x01fcfcfcu ^ (seed & 0x03000000u), tb = 0xfc01fcfcu, up = V::splat(2041), diag0 = V::splat(2048);
     for (int s = 0; s < steps; ++s) {
         uint32_t diag = diag0, Ed = up;
 #pragma unroll
         for (int k = 0; k < R; ++k) {
             const uint32_t sc = prmt(ta, tb, Sel[k]);
             const uint32_t tt = V::addmax(diag, sc, Fr[k]);
-            const uint32_t h = V::hmax_global(tt, Ed, FLOOR);
+            const uint32_t h = V::hmax(tt, Ed, CLAMP);
             diag = H[k];
             H[k] = h;
-            const uint32_t hoe = V::add(h, GOE);
-            Fr[k] = V::addmax(Fr[k], EXT, hoe);
-            Ed = V::addmax(Ed, EXT, hoe);
+            const uint32_t hoe = V::subc(h, GOEA);
+            Fr[k] = V::max2(V::subc(Fr[k], EXTA), hoe);
+            Ed = V::max2(V::subc(Ed, EXTA), hoe);
         }
         diag0 = H[R - 1];
         up = Ed;
@@ -411,7 +428,8 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
         cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device_ordinal) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
-        cudaEventCreate(&c->ev2) != cudaSuccess || cudaEventCreate(&c->ev3) != cudaSuccess) {
+        cudaEventCreate(&c->ev2) != cudaSuccess || cudaEventCreate(&c->ev3) != cudaSuccess ||
+        cudaEventCreate(&c->ev_dp0) != cudaSuccess || cudaEventCreate(&c->ev_dp1) != cudaSuccess) {
         cudaGetLastError();
         delete c;
         return PA_ERR_CUDA;
@@ -422,6 +440,9 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
         for (int k = 0; k < 3; ++k) c->G[k] = g;
     }
     if (c->opt.rows_per_thread && c->opt.rows_per_thread != kR) { pa_destroy(c); return PA_ERR_UNSUPPORTED; }
+    if (c->opt.kernel_variant >= 0 && c->opt.kernel_variant <= 2)
+        for (int k = 0; k < 3; ++k) c->variant[k] = c->opt.kernel_variant;
+    else if (c->opt.kernel_variant != -1) { pa_destroy(c); return PA_ERR_INVALID_ARGUMENT; }
     warm_occupancy();
     *out = c;
     return PA_OK;
@@ -442,6 +463,8 @@ pa_status pa_destroy(pa_ctx *c)
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->ev2) cudaEventDestroy(c->ev2);
     if (c->ev3) cudaEventDestroy(c->ev3);
+    if (c->ev_dp0) cudaEventDestroy(c->ev_dp0);
+    if (c->ev_dp1) cudaEventDestroy(c->ev_dp1);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return PA_OK;
@@ -518,6 +541,8 @@ pa_status pa_align_batch(pa_ctx *ctx, const pa_config *config, const uint8_t *se
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
         stats->device_ms = ms;
+        if (cudaEventElapsedTime(&ms, ctx->ev_dp0, ctx->ev_dp1) == cudaSuccess) stats->dp_ms = ms;
+        cudaGetLastError();
         stats->cells = ps.cells;
         stats->pairs_s16 = ps.n_class[K_S16] - ctr[4];
         stats->pairs_s32 = ps.n_class[K_S32] + ctr[4];

@@ -1,9 +1,9 @@
 // pa_dp.cuh -- the affine-gap (Gotoh) score DP kernel for sm_103a.
 //
 // One "group" of G consecutive lanes of a warp (G = 1, 2, ..., 32) computes the
-// DP matrix of one pair (s32 lanes) or of two pairs at once (s16x2 lanes: pair A
-// in the low halfword, pair B in the high halfword of every register).  The
-// recurrence is the reference's compute_cell
+// DP matrix of two pairs at once in s16x2 lanes (pair A in the low halfword,
+// pair B in the high halfword of every register) or of one pair in s32 lanes.
+// The recurrence is the reference's compute_cell
 // (include/pairwise_aligner/affine/affine_dp_algorithm.hpp:149-155):
 //     best = max(diag + s(a,b), vgap, hgap)          [local: max(diag + s, 0) first,
 //                                                     dp_matrix_local.hpp:39-47]
@@ -11,29 +11,35 @@
 // with the border cells of affine_initialisation_strategy.hpp:38-51.
 //
 // Layout of the work: sequence2 ("held") runs down the rows, sequence1
-// ("streamed") along the columns.  Thread t of a group holds rows
-// [t*R, t*R + R) of the current pass in registers (H and the rightward gap per
-// row, plus a byte-permute selector that encodes the row's base); the group
-// sweeps the columns as an anti-diagonal wavefront: at step s thread t computes
-// column s - t + 1 and hands the bottom H and downward gap of its strip to
-// thread t+1 with __shfl_up_sync.  Rows beyond G*R are covered by further
-// passes; the last thread spills its bottom row per column to the pass-boundary
-// scratch (8 bytes per column), where thread 0 of the next pass reads it.
+// ("streamed") along the columns.  Thread t of a group holds RA consecutive rows
+// of the current pass in registers (H and the rightward gap per row, plus a
+// byte-permute selector that encodes the row's base); the group sweeps the
+// columns as an anti-diagonal wavefront: at step s thread t computes column
+// s - t + 1 and hands the bottom H and the downward gap of its strip to thread
+// t+1 with __shfl_up_sync.  Rows beyond G*R are covered by further passes; the
+// last thread spills its bottom row per column to the pass-boundary scratch
+// (8 bytes per column), where thread 0 of the next pass reads it.
 //
-// Scores: the streamed base of each lane selects a 4-byte table
-// (match in the byte of its 2-bit code, mismatch elsewhere); one PRMT with the
-// row's selector yields the packed, sign-extended scores of both lanes.
-// Arithmetic: DPX __viaddmax / __vimax3(_relu) in s16x2 or s32 form.
+// Instruction budget (sm_103: PRMT, LOP3 and the 3-operand DPX forms take two
+// ALU issue slots, the 2-operand __vmaxs2 one, integer adds go to another pipe);
+// per register (two cells of s16x2 lanes):
+//     s  = PRMT(table_a, table_b, selector)            score of both lanes
+//     t  = VIADDMAX(diag, s, hgap)                      max(diag + s, hgap)
+//     H  = VIMAX3(t, vgap, clamp)                       local 0 / global floor
+//     Ho = H - |open+ext|                               IADD, borrow free
+//     hgap = VMAX(hgap - |ext|, Ho);  vgap = VMAX(vgap - |ext|, Ho)
+// s16x2 values are stored with a per-group offset K so that every halfword
+// stays in [0, 32767]: subtracting a constant never borrows across halfwords and
+// signed DPX comparisons stay valid.  Local: true 0 == K.  Global: the clamp at
+// 2048 is a floor; a result above floor + smax * min(m, n) cannot have been
+// influenced by a clamp and is exact, anything else is recomputed in s32.
 //
 // Tracking (the reference trackers, tracker/*.hpp):
 //   local  -- running column maximum per strip; on a strict improvement the
-//             strip's H column is kept, so the end is the smallest column i,
-//             then the smallest row j of the maximum (order independent).
+//             strip's H column is stored to shared memory, so the end is the
+//             smallest column i, then the smallest row j of the maximum.
 //   global -- H(m, n) is read where it is computed; free trailing gaps also
 //             scan the last row (i = m) and the last column (j = n).
-// s16 global lanes clamp every H at `floor16` from below, which keeps all adds
-// inside int16; a result above floor16 + smax * min(m, n) cannot have been
-// influenced by a clamp and is exact, anything else is recomputed in s32.
 #pragma once
 #include "pa_common.cuh"
 
@@ -47,7 +53,7 @@ struct L16 {
     static constexpr uint8_t WIDTH = 16;
     static __device__ __forceinline__ uint32_t splat(int32_t x)
     {
-        uint32_t h = (uint16_t)(int16_t)x;
+        const uint32_t h = (uint16_t)(int16_t)x;
         return h | (h << 16);
     }
     static __device__ __forceinline__ int32_t get(uint32_t v, int l)
@@ -58,37 +64,26 @@ struct L16 {
     {
         return __viaddmax_s16x2(a, b, c);
     }
-    static __device__ __forceinline__ uint32_t add(uint32_t a, uint32_t b)
+    static __device__ __forceinline__ uint32_t hmax(uint32_t t, uint32_t e, uint32_t clamp)
     {
-        return __viaddmax_s16x2(a, b, 0x80008000u);
+        return __vimax3_s16x2(t, e, clamp);
     }
-    static __device__ __forceinline__ uint32_t hmax_local(uint32_t t, uint32_t e, uint32_t)
-    {
-        return __vimax_s16x2_relu(t, e);
-    }
-    static __device__ __forceinline__ uint32_t hmax_global(uint32_t t, uint32_t e, uint32_t fl)
-    {
-        return __vimax3_s16x2(t, e, fl);
-    }
+    static __device__ __forceinline__ uint32_t max2(uint32_t a, uint32_t b) { return __vmaxs2(a, b); }
     static __device__ __forceinline__ uint32_t max3(uint32_t a, uint32_t b, uint32_t c)
     {
         return __vimax3_s16x2(a, b, c);
     }
-    // best = max(best, c) per lane; returns an all-ones mask over the lanes where c > old best.
-    static __device__ __forceinline__ uint32_t improve(uint32_t &best, uint32_t c)
-    {
-        const uint32_t gt = __vcmpgts2(c, best);   // 0xffff per halfword where c > best
-        best = __vmaxs2(best, c);
-        return gt;
-    }
-    static __device__ __forceinline__ bool lane_bit(uint32_t mask, int l) { return (mask >> (16 * l)) & 1u; }
+    // x - c in both halfwords; cabs2 = |c| * 0x10001; halfwords of x are >= |c|.
+    static __device__ __forceinline__ uint32_t subc(uint32_t x, uint32_t cabs2) { return x - cabs2; }
+    static __device__ __forceinline__ uint32_t cabs(int32_t c) { return (uint32_t)(c < 0 ? -c : c) * 0x10001u; }
+    static __device__ __forceinline__ bool improved(uint32_t x, int l) { return (l ? (x >> 16) : (x & 0xffffu)) != 0; }
     // Byte-permute selector of a held row.  Low halfword <- table byte `ca` of lane A
     // (bytes 0-3) sign-extended, high halfword <- byte 4+cb of lane B.  A padded row
     // (code < 0) replicates the sign of a table byte: its score is 0 or -1.
     static __device__ __forceinline__ uint32_t selector(int ca, int cb)
     {
-        uint32_t lo = ca < 0 ? 0x88u : ((uint32_t)ca | (((uint32_t)ca | 8u) << 4));
-        uint32_t hi = cb < 0 ? 0xCCu : ((4u + (uint32_t)cb) | (((4u + (uint32_t)cb) | 8u) << 4));
+        const uint32_t lo = ca < 0 ? 0x88u : ((uint32_t)ca | (((uint32_t)ca | 8u) << 4));
+        const uint32_t hi = cb < 0 ? 0xCCu : ((4u + (uint32_t)cb) | (((4u + (uint32_t)cb) | 8u) << 4));
         return lo | (hi << 8);
     }
 };
@@ -100,32 +95,24 @@ struct L32 {
     static __device__ __forceinline__ int32_t get(uint32_t v, int) { return (int32_t)v; }
     static __device__ __forceinline__ uint32_t addmax(uint32_t a, uint32_t b, uint32_t c)
     {
-        return (uint32_t)__viaddmax_s32((int)a, (int)b, (int)c);
+        return (uint32_t)max((int)(a + b), (int)c);
     }
-    static __device__ __forceinline__ uint32_t add(uint32_t a, uint32_t b) { return a + b; }
-    static __device__ __forceinline__ uint32_t hmax_local(uint32_t t, uint32_t e, uint32_t)
+    static __device__ __forceinline__ uint32_t hmax(uint32_t t, uint32_t e, uint32_t clamp)
     {
-        return (uint32_t)__vimax_s32_relu((int)t, (int)e);
+        return (uint32_t)__vimax3_s32((int)t, (int)e, (int)clamp);
     }
-    static __device__ __forceinline__ uint32_t hmax_global(uint32_t t, uint32_t e, uint32_t)
-    {
-        return (uint32_t)max((int)t, (int)e);
-    }
+    static __device__ __forceinline__ uint32_t max2(uint32_t a, uint32_t b) { return (uint32_t)max((int)a, (int)b); }
     static __device__ __forceinline__ uint32_t max3(uint32_t a, uint32_t b, uint32_t c)
     {
         return (uint32_t)__vimax3_s32((int)a, (int)b, (int)c);
     }
-    static __device__ __forceinline__ uint32_t improve(uint32_t &best, uint32_t c)
-    {
-        const bool gt = (int)c > (int)best;
-        best = gt ? c : best;
-        return gt ? 0xffffffffu : 0u;
-    }
-    static __device__ __forceinline__ bool lane_bit(uint32_t mask, int) { return mask != 0u; }
+    static __device__ __forceinline__ uint32_t subc(uint32_t x, uint32_t cabs) { return x - cabs; }
+    static __device__ __forceinline__ uint32_t cabs(int32_t c) { return (uint32_t)(c < 0 ? -c : c); }
+    static __device__ __forceinline__ bool improved(uint32_t x, int) { return x != 0; }
     static __device__ __forceinline__ uint32_t selector(int ca, int)
     {
         if (ca < 0) return 0x8888u;
-        uint32_t c = (uint32_t)ca, s = c | 8u;
+        const uint32_t c = (uint32_t)ca, s = c | 8u;
         return c | (s << 4) | (s << 8) | (s << 12);
     }
 };
@@ -136,15 +123,228 @@ __device__ __forceinline__ bool better(int32_t s, int32_t i, int32_t j, int32_t 
     return s > bs || (s == bs && (i < bi || (i == bi && j < bj)));
 }
 
-constexpr int kChunk = 4;   // rows per guarded chunk of the register strip
+constexpr int kChunk = 4;      // granularity of the rows a thread holds in a short last pass
+constexpr int kBlock = 256;    // threads per block of every DP launch
+
+// Everything one group needs to know about its current work unit.
+struct GroupWork {
+    uint32_t id[2];
+    uint64_t qoff[2], toff[2];
+    int32_t m[2], n[2];
+    int32_t ms, nh, passes, rows_full;
+    bool has_b;
+    uint32_t K, CLAMP;         // offset and clamp of the stored values
+    int32_t Kt, clampt;        // the same as true-score integers
+    int32_t floor_true;        // global s16 lanes: true value of the clamp
+    const uint32_t *qt[2];
+    Cell *buf;
+    int32_t cs[2], ci[2], cj[2];   // candidate (score, end1, end2) per lane
+};
+
+template <class V>
+__device__ __forceinline__ uint32_t stored(const GroupWork &w, int32_t true_value)
+{
+    int32_t x = true_value + w.Kt;
+    if (V::LANES == 2) x = max(x, w.clampt);
+    return V::splat(x);
+}
+
+template <class V, int R, int RA, int MODE, bool GEN, int VAR>
+__device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, GroupWork &w, int p, int t, int G,
+                                         unsigned gmask, uint4 *snap)
+{
+    constexpr int NL = V::LANES;
+    const int32_t j0 = p * w.rows_full + t * RA;   // rows j0+1 .. j0+RA (1-based)
+    const uint32_t GOEA = V::cabs(P.gap_open + P.gap_ext);
+    const uint32_t EXTA = V::cabs(P.gap_ext);
+    const uint32_t CLAMP = w.CLAMP;
+
+    uint32_t H[RA], Fr[RA], Sel[RA];
+#pragma unroll
+    for (int k = 0; k < RA; ++k) {
+        const int32_t j = j0 + k;                     // 0-based index into sequence2
+        int c[2];
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            if (GEN) c[l] = (j < w.n[l]) ? (int)L.seq2[w.toff[l] + j] : 0x100;
+            else c[l] = (j < w.n[l]) ? (int)dna_code(L.seq2[w.toff[l] + j]) : -1;
+        }
+        Sel[k] = GEN ? (uint32_t)c[0] : V::selector(c[0], c[1]);
+        H[k] = stored<V>(w, border(P, P.first_row_free, (int64_t)j + 1));
+        Fr[k] = V::subc(H[k], GOEA);
+    }
+    uint32_t prevH = stored<V>(w, border(P, P.first_row_free, j0));
+    uint32_t topH = prevH;                              // thread 0, pass 0: H(i-1, 0)
+    const uint32_t step1 = P.first_column_free ? 0u : V::cabs(P.gap_open + P.gap_ext);
+    const uint32_t stepn = P.first_column_free ? 0u : EXTA;
+    uint32_t outH = 0, outE = 0, best = w.K;
+    int32_t bi[2] = {0, 0};
+    int32_t own_k[2], own_t[2];
+    bool own_p[2];
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {                     // where row n[l] lives
+        const int32_t pl = (w.n[l] - 1) / w.rows_full;
+        own_p[l] = (pl == p);
+        const int32_t r = (w.n[l] - 1) - pl * w.rows_full;
+        own_t[l] = r / RA;
+        own_k[l] = r - own_t[l] * RA;
+    }
+    const int32_t ms = w.ms;
+    const bool last_pass = p + 1 == w.passes;
+    // next column's score tables, loaded one step ahead
+    uint32_t nta = 0, ntb = 0;
+    auto load_tables = [&](int32_t col, uint32_t &a, uint32_t &b) {
+        if (GEN) {
+            a = (col <= w.m[0]) ? (uint32_t)L.seq1[w.qoff[0] + col - 1] : 0x200u;
+            b = a;
+        } else {
+            a = __ldg(w.qt[0] + min(col - 1, w.m[0]));
+            b = NL == 2 ? __ldg(w.qt[1] + min(col - 1, w.m[1])) : a;
+        }
+    };
+    Cell nbuf = Cell{0u, 0u};                        // thread 0, pass > 0: next boundary cell
+    if (t == 0 && p > 0) nbuf = w.buf[1];
+    auto step = [&](int32_t i, bool active) {
+        uint32_t upH = __shfl_up_sync(gmask, outH, 1, G);
+        uint32_t upE = __shfl_up_sync(gmask, outE, 1, G);
+        if (!active) return;
+        if (t == 0) {
+            if (p == 0) {
+                topH = V::max2(V::subc(topH, i == 1 ? step1 : stepn), CLAMP);
+                upH = topH;
+                upE = V::subc(topH, GOEA);
+            } else {
+                upH = nbuf.h;
+                upE = nbuf.e;
+                if (i < ms) nbuf = w.buf[i + 1];
+            }
+        }
+        const uint32_t ta = nta, tb = ntb;
+        if (i < ms) load_tables(i + 1, nta, ntb);
+        uint32_t diag = prevH, Ed = upE;
+#pragma unroll
+        for (int k = 0; k < RA; ++k) {
+            uint32_t sc;
+            if (GEN) {
+                const uint32_t x = Sel[k];
+                sc = (x == ta) ? (uint32_t)P.match : (((x | ta) >> 8) ? (uint32_t)P.spad : (uint32_t)P.mismatch);
+            } else {
+                sc = prmt(ta, tb, Sel[k]);
+            }
+            const uint32_t tt = V::addmax(diag, sc, Fr[k]);
+            diag = H[k];
+            if (VAR == 0) {
+                const uint32_t h = V::hmax(tt, Ed, CLAMP);
+                H[k] = h;
+                const uint32_t hoe = V::subc(h, GOEA);
+                Fr[k] = V::max2(V::subc(Fr[k], EXTA), hoe);
+                Ed = V::max2(V::subc(Ed, EXTA), hoe);
+            } else {
+                // vgap' = max(vgap + ext, max(t, clamp) + open + ext): H leaves the serial chain
+                const uint32_t x = V::max2(tt, CLAMP);
+                const uint32_t h = V::max2(x, Ed);
+                H[k] = h;
+                Fr[k] = V::max2(V::subc(Fr[k], EXTA), V::subc(h, GOEA));
+                Ed = V::max2(V::subc(Ed, EXTA), V::subc(x, GOEA));
+            }
+        }
+        prevH = upH;
+        outH = H[RA - 1];
+        outE = Ed;
+        if (t == G - 1 && !last_pass) w.buf[i] = Cell{outH, outE};
+
+        if (MODE == M_LOCAL) {
+            uint32_t cm = H[0];
+#pragma unroll
+            for (int k = 1; k < RA; k += 2) cm = V::max3(cm, H[k], H[k + 1 < RA ? k + 1 : k]);
+            const uint32_t nb = V::max2(best, cm);
+            const uint32_t x = nb ^ best;
+            best = nb;
+#pragma unroll
+            for (int l = 0; l < NL; ++l) {
+                if (x != 0u && V::improved(x, l)) {
+                    bi[l] = i;
+#pragma unroll
+                    for (int v = 0; v < RA / 4; ++v)
+                        snap[(l * (R / 4) + v) * kBlock + threadIdx.x] =
+                            make_uint4(H[4 * v], H[4 * v + 1], H[4 * v + 2], H[4 * v + 3]);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int l = 0; l < NL; ++l) {
+                if (l == 1 && !w.has_b) continue;
+                if (MODE == M_GLOBAL_FREE && P.last_column_free && own_p[l] && t == own_t[l] && i <= w.m[l]) {
+                    uint32_t v = H[0];
+#pragma unroll
+                    for (int k = 1; k < RA; ++k)
+                        if (own_k[l] == k) v = H[k];
+                    const int32_t xs = V::get(v, l) - w.Kt;
+                    if (better(xs, i, w.n[l], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = xs; w.ci[l] = i; w.cj[l] = w.n[l]; }
+                }
+                if (i == w.m[l]) {
+                    if (MODE == M_GLOBAL_FREE && P.last_row_free) {
+#pragma unroll
+                        for (int k = 0; k < RA; ++k) {
+                            const int32_t j = j0 + k + 1;
+                            if (j <= w.n[l]) {
+                                const int32_t xs = V::get(H[k], l) - w.Kt;
+                                if (better(xs, i, j, w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = xs; w.ci[l] = i; w.cj[l] = j; }
+                            }
+                        }
+                    } else if (own_p[l] && t == own_t[l]) {
+                        uint32_t v = H[0];
+#pragma unroll
+                        for (int k = 1; k < RA; ++k)
+                            if (own_k[l] == k) v = H[k];
+                        const int32_t xs = V::get(v, l) - w.Kt;
+                        if (better(xs, i, w.n[l], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = xs; w.ci[l] = i; w.cj[l] = w.n[l]; }
+                    }
+                }
+            }
+        }
+    };
+    // fill: thread t starts at step t (steps 0..G-1); steady: every thread active; drain
+    if (t == 0) load_tables(1, nta, ntb);
+    const int32_t fill_end = min(G, ms + G - 1);
+    int s = 0;
+    for (; s < fill_end; ++s) {
+        const int32_t i = s - t + 1;
+        if (i == 1 && t > 0) load_tables(1, nta, ntb);
+        step(i, i >= 1 && i <= ms);
+    }
+    for (; s < ms; ++s) step(s - t + 1, true);
+    for (; s < ms + G - 1; ++s) {
+        const int32_t i = s - t + 1;
+        step(i, i >= 1 && i <= ms);
+    }
+    if (MODE == M_LOCAL) {
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
+            const int32_t b = V::get(best, l);
+            if (b > w.Kt) {
+                int32_t kk = 0;
+                for (int v = RA / 4 - 1; v >= 0; --v) {
+                    const uint4 q = snap[(l * (R / 4) + v) * kBlock + threadIdx.x];
+                    if (V::get(q.w, l) == b) kk = 4 * v + 3;
+                    if (V::get(q.z, l) == b) kk = 4 * v + 2;
+                    if (V::get(q.y, l) == b) kk = 4 * v + 1;
+                    if (V::get(q.x, l) == b) kk = 4 * v;
+                }
+                const int32_t xs = b - w.Kt, j = j0 + kk + 1;
+                if (better(xs, bi[l], j, w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = xs; w.ci[l] = bi[l]; w.cj[l] = j; }
+            }
+        }
+    }
+}
 
 // GEN = byte-compare scoring (any bytes, any int32 scores), always with L32 lanes.
-template <class V, int R, int MODE, bool GEN>
-__global__ void __launch_bounds__(256) dp_kernel(DpLaunch L, DpParams P)
+template <class V, int R, int MODE, bool GEN, int VAR, int MINB = 2>
+__global__ void __launch_bounds__(kBlock, MINB) dp_kernel(DpLaunch L, DpParams P)
 {
-    static_assert(R % kChunk == 0, "R must be a multiple of the chunk");
+    static_assert(R % kChunk == 0 && R <= 32, "R must be a multiple of the chunk");
     constexpr int NL = V::LANES;
-    constexpr int NCH = R / kChunk;
+    __shared__ uint4 snap_store[MODE == M_LOCAL ? NL * (R / 4) * kBlock : 1];
     const int lane = threadIdx.x & 31;
     const int G = L.G;
     const int t = lane & (G - 1);
@@ -155,12 +355,6 @@ __global__ void __launch_bounds__(256) dp_kernel(DpLaunch L, DpParams P)
     const uint32_t ppw = (uint32_t)(32 / G) * NL;   // pairs per warp unit
     const uint32_t n_units = (count + ppw - 1) / ppw;
 
-    const uint32_t GOE = V::splat(P.gap_open + P.gap_ext);
-    const uint32_t EXT = V::splat(P.gap_ext);
-    const uint32_t FLOOR = V::splat(P.floor16);
-    const bool clamp16 = (NL == 2) && MODE != M_LOCAL;
-    const uint32_t PADTAB = 0x80808080u;
-
     for (;;) {
         uint32_t u = 0;
         if (lane == 0) u = atomicAdd(L.unit_counter, 1u);
@@ -170,194 +364,56 @@ __global__ void __launch_bounds__(256) dp_kernel(DpLaunch L, DpParams P)
         const uint32_t first = u * ppw + (uint32_t)g * NL;
         if (first >= count) continue;                // idle group in the last unit
 
-        uint32_t id[2];
-        id[0] = order[first];
-        const bool has_b = NL == 2 && first + 1 < count;
-        id[1] = has_b ? order[first + 1] : id[0];
-        uint64_t qoff[2], toff[2];
-        int32_t m[2], n[2];
+        GroupWork w;
+        w.id[0] = order[first];
+        w.has_b = NL == 2 && first + 1 < count;
+        w.id[1] = w.has_b ? order[first + 1] : w.id[0];
 #pragma unroll
         for (int l = 0; l < 2; ++l) {
-            qoff[l] = L.off1[id[l]];
-            m[l] = (int32_t)(L.off1[id[l] + 1] - qoff[l]);
-            toff[l] = L.off2[id[l]];
-            n[l] = (int32_t)(L.off2[id[l] + 1] - toff[l]);
+            w.qoff[l] = L.off1[w.id[l]];
+            w.m[l] = (int32_t)(L.off1[w.id[l] + 1] - w.qoff[l]);
+            w.toff[l] = L.off2[w.id[l]];
+            w.n[l] = (int32_t)(L.off2[w.id[l] + 1] - w.toff[l]);
+            w.qt[l] = L.qtab + w.qoff[l] + w.id[l];
+            w.cs[l] = MODE == M_LOCAL ? 0 : INT32_MIN;
+            w.ci[l] = 0;
+            w.cj[l] = 0;
         }
-        const int32_t ms = NL == 2 ? max(m[0], m[1]) : m[0];
-        const int32_t nh = NL == 2 ? max(n[0], n[1]) : n[0];
-        const int32_t rows_full = G * R;
-        const int32_t passes = (nh + rows_full - 1) / rows_full;
-        const int owner = (NL == 2 && m[1] > m[0]) ? 1 : 0;
-        Cell *buf = L.boundary + (L.off1[id[owner]] + id[owner]);
-        const uint32_t *qt[2];
-#pragma unroll
-        for (int l = 0; l < 2; ++l) qt[l] = L.qtab + qoff[l] + id[l];
-
-        int32_t cs[2], ci[2], cj[2];
-#pragma unroll
-        for (int l = 0; l < 2; ++l) { cs[l] = MODE == M_LOCAL ? 0 : INT32_MIN; ci[l] = 0; cj[l] = 0; }
-
-        for (int p = 0; p < passes; ++p) {
-            // rows of this pass: the last pass keeps only the chunks it needs
-            const int32_t rem = nh - p * rows_full;
-            const int32_t rpt = rem >= rows_full ? R : ((rem + G * kChunk - 1) / (G * kChunk)) * kChunk;
-            const int32_t nch = rpt / kChunk;
-            const int32_t pass_base = p * rows_full;
-            const int32_t j0 = pass_base + t * rpt;   // rows j0+1 .. j0+rpt (1-based)
-
-            uint32_t H[R], Fr[R], Sel[R], Snap[R];
-#pragma unroll
-            for (int k = 0; k < R; ++k) {
-                const int32_t j = j0 + k;              // 0-based index into sequence2
-                int c[2];
-#pragma unroll
-                for (int l = 0; l < 2; ++l) {
-                    if (GEN) c[l] = (k < rpt && j < n[l]) ? (int)L.seq2[toff[l] + j] : 0x100;
-                    else c[l] = (k < rpt && j < n[l]) ? (int)dna_code(L.seq2[toff[l] + j]) : -1;
-                }
-                Sel[k] = GEN ? (uint32_t)c[0] : V::selector(c[0], c[1]);
-                int32_t h = border(P, P.first_row_free, (int64_t)j + 1);
-                if (clamp16) h = max(h, P.floor16);
-                H[k] = V::splat(h);
-                Fr[k] = V::add(H[k], GOE);
-                Snap[k] = 0;
-            }
-            int32_t hp = border(P, P.first_row_free, j0);
-            if (clamp16) hp = max(hp, P.floor16);
-            uint32_t prevH = V::splat(hp);
-            uint32_t outH = 0, outE = 0, best = 0;
-            int32_t bi[2] = {0, 0};
-            int32_t own_k[2], own_t[2], own_p[2];
-#pragma unroll
-            for (int l = 0; l < 2; ++l) {            // where row n[l] lives
-                own_p[l] = (n[l] - 1) / rows_full;
-                const int32_t r = (n[l] - 1) - own_p[l] * rows_full;
-                const int32_t rr = (own_p[l] == p) ? rpt : R;
-                own_t[l] = r / rr;
-                own_k[l] = r - own_t[l] * rr;
-            }
-
-            const int32_t steps = ms + G - 1;
-            for (int s = 0; s < steps; ++s) {
-                const int32_t i = s - t + 1;          // 1-based column of this thread
-                uint32_t upH = __shfl_up_sync(gmask, outH, 1, G);
-                uint32_t upE = __shfl_up_sync(gmask, outE, 1, G);
-                if (i < 1 || i > ms) continue;
-                if (t == 0) {
-                    if (p == 0) {
-                        int32_t h = border(P, P.first_column_free, i);
-                        if (clamp16) h = max(h, P.floor16);
-                        upH = V::splat(h);
-                        upE = V::add(upH, GOE);
-                    } else {
-                        const Cell c = buf[i];
-                        upH = c.h;
-                        upE = c.e;
-                    }
-                }
-                // streamed base of each lane -> score table (or raw byte for GEN)
-                uint32_t ta, tb;
-                if (GEN) {
-                    ta = (i <= m[0]) ? (uint32_t)L.seq1[qoff[0] + i - 1] : 0x200u;
-                    tb = ta;
-                } else {
-                    ta = __ldg(qt[0] + min(i - 1, m[0]));
-                    tb = NL == 2 ? __ldg(qt[1] + min(i - 1, m[1])) : ta;
-                }
-                uint32_t diag = prevH, Ed = upE;
-#pragma unroll
-                for (int k = 0; k < R; ++k) {
-                    if (k % kChunk == 0 && k / kChunk >= nch) break;
-                    uint32_t sc;
-                    if (GEN) {
-                        const uint32_t x = Sel[k];
-                        sc = (x == ta) ? (uint32_t)P.match
-                                       : (((x | ta) >> 8) ? (uint32_t)P.spad : (uint32_t)P.mismatch);
-                    } else {
-                        sc = prmt(ta, tb, Sel[k]);
-                    }
-                    const uint32_t tt = V::addmax(diag, sc, Fr[k]);
-                    const uint32_t h = MODE == M_LOCAL ? V::hmax_local(tt, Ed, FLOOR) : V::hmax_global(tt, Ed, FLOOR);
-                    diag = H[k];
-                    H[k] = h;
-                    const uint32_t hoe = V::add(h, GOE);
-                    Fr[k] = V::addmax(Fr[k], EXT, hoe);
-                    Ed = V::addmax(Ed, EXT, hoe);
-                }
-                prevH = upH;
-                uint32_t last = H[R - 1];
-#pragma unroll
-                for (int c = 1; c < NCH; ++c)
-                    if (nch == c) last = H[c * kChunk - 1];
-                outH = last;
-                outE = Ed;
-                if (t == G - 1 && p + 1 < passes) buf[i] = Cell{outH, outE};
-
-                if (MODE == M_LOCAL) {
-                    uint32_t cm = 0;                  // local H >= 0
-#pragma unroll
-                    for (int c = 0; c < NCH; ++c) {
-                        if (c >= nch) break;
-                        cm = V::max3(cm, H[c * kChunk], H[c * kChunk + 1]);
-                        cm = V::max3(cm, H[c * kChunk + 2], H[c * kChunk + 3]);
-                    }
-                    const uint32_t mask = V::improve(best, cm);
-#pragma unroll
-                    for (int k = 0; k < R; ++k) {
-                        if (k % kChunk == 0 && k / kChunk >= nch) break;
-                        Snap[k] = (H[k] & mask) | (Snap[k] & ~mask);
-                    }
-#pragma unroll
-                    for (int l = 0; l < NL; ++l)
-                        if (V::lane_bit(mask, l)) bi[l] = i;
-                } else {
-#pragma unroll
-                    for (int l = 0; l < NL; ++l) {
-                        if (l == 1 && !has_b) continue;
-                        if (MODE == M_GLOBAL_FREE && P.last_column_free && p == own_p[l] && t == own_t[l] &&
-                            i <= m[l]) {
-                            uint32_t v = H[0];
-#pragma unroll
-                            for (int k = 1; k < R; ++k)
-                                if (own_k[l] == k) v = H[k];
-                            const int32_t x = V::get(v, l);
-                            if (better(x, i, n[l], cs[l], ci[l], cj[l])) { cs[l] = x; ci[l] = i; cj[l] = n[l]; }
-                        }
-                        if (i == m[l]) {
-                            if (MODE == M_GLOBAL_FREE && P.last_row_free) {
-#pragma unroll
-                                for (int k = 0; k < R; ++k) {
-                                    const int32_t j = j0 + k + 1;
-                                    if (k < rpt && j <= n[l]) {
-                                        const int32_t x = V::get(H[k], l);
-                                        if (better(x, i, j, cs[l], ci[l], cj[l])) { cs[l] = x; ci[l] = i; cj[l] = j; }
-                                    }
-                                }
-                            } else if (p == own_p[l] && t == own_t[l]) {
-                                uint32_t v = H[0];
-#pragma unroll
-                                for (int k = 1; k < R; ++k)
-                                    if (own_k[l] == k) v = H[k];
-                                const int32_t x = V::get(v, l);
-                                if (better(x, i, n[l], cs[l], ci[l], cj[l])) { cs[l] = x; ci[l] = i; cj[l] = n[l]; }
-                            }
-                        }
-                    }
-                }
-            }
+        w.ms = NL == 2 ? max(w.m[0], w.m[1]) : w.m[0];
+        w.nh = NL == 2 ? max(w.n[0], w.n[1]) : w.n[0];
+        w.rows_full = G * R;
+        w.passes = (w.nh + w.rows_full - 1) / w.rows_full;
+        const uint32_t owner = (NL == 2 && w.m[1] > w.m[0]) ? w.id[1] : w.id[0];
+        w.buf = L.boundary + (L.off1[owner] + owner);
+        if (NL == 2) {
             if (MODE == M_LOCAL) {
-#pragma unroll
-                for (int l = 0; l < NL; ++l) {
-                    const int32_t b = V::get(best, l);
-                    if (b > 0) {
-                        int32_t kk = -1;
-#pragma unroll
-                        for (int k = R - 1; k >= 0; --k)
-                            if (k < rpt && V::get(Snap[k], l) == b) kk = k;
-                        const int32_t j = j0 + kk + 1;
-                        if (better(b, bi[l], j, cs[l], ci[l], cj[l])) { cs[l] = b; ci[l] = bi[l]; cj[l] = j; }
-                    }
-                }
+                w.Kt = 2048;
+                w.clampt = 2048;
+                w.floor_true = 0;
+            } else {
+                const int32_t ub = P.smax * max(min(w.m[0], w.n[0]), min(w.m[1], w.n[1]));
+                w.Kt = 32767 - 512 - ub;
+                w.clampt = 2048;
+                w.floor_true = 2048 - w.Kt;
+            }
+            w.K = V::splat(w.Kt);
+            w.CLAMP = V::splat(w.clampt);
+        } else {
+            w.Kt = 0;
+            w.clampt = MODE == M_LOCAL ? 0 : INT32_MIN;
+            w.floor_true = INT32_MIN;
+            w.K = 0;
+            w.CLAMP = (uint32_t)w.clampt;
+        }
+
+        for (int p = 0; p < w.passes; ++p) {
+            const int32_t rem = w.nh - p * w.rows_full;
+            const int32_t rpt = rem >= w.rows_full ? R : ((rem + G * kChunk - 1) / (G * kChunk)) * kChunk;
+            switch (rpt / kChunk) {
+            case 1: run_pass<V, R, 4, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
+            case 2: run_pass<V, R, 8, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
+            case 3: run_pass<V, R, 12, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
+            default: run_pass<V, R, R, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
             }
             __syncwarp(gmask);
         }
@@ -366,41 +422,42 @@ __global__ void __launch_bounds__(256) dp_kernel(DpLaunch L, DpParams P)
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
             for (int off = G >> 1; off >= 1; off >>= 1) {
-                const int32_t os = __shfl_xor_sync(gmask, cs[l], off, G);
-                const int32_t oi = __shfl_xor_sync(gmask, ci[l], off, G);
-                const int32_t oj = __shfl_xor_sync(gmask, cj[l], off, G);
-                if (better(os, oi, oj, cs[l], ci[l], cj[l])) { cs[l] = os; ci[l] = oi; cj[l] = oj; }
+                const int32_t os = __shfl_xor_sync(gmask, w.cs[l], off, G);
+                const int32_t oi = __shfl_xor_sync(gmask, w.ci[l], off, G);
+                const int32_t oj = __shfl_xor_sync(gmask, w.cj[l], off, G);
+                if (better(os, oi, oj, w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = os; w.ci[l] = oi; w.cj[l] = oj; }
             }
         }
         if (t == 0) {
 #pragma unroll
             for (int l = 0; l < NL; ++l) {
-                if (l == 1 && !has_b) continue;
+                if (l == 1 && !w.has_b) continue;
                 if (MODE == M_GLOBAL_FREE) {
                     if (P.last_column_free) {            // H(0, n)
-                        const int32_t x = border(P, P.first_row_free, n[l]);
-                        if (better(x, 0, n[l], cs[l], ci[l], cj[l])) { cs[l] = x; ci[l] = 0; cj[l] = n[l]; }
+                        const int32_t x = border(P, P.first_row_free, w.n[l]);
+                        if (better(x, 0, w.n[l], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = x; w.ci[l] = 0; w.cj[l] = w.n[l]; }
                     }
                     if (P.last_row_free) {               // H(m, 0)
-                        const int32_t x = border(P, P.first_column_free, m[l]);
-                        if (better(x, m[l], 0, cs[l], ci[l], cj[l])) { cs[l] = x; ci[l] = m[l]; cj[l] = 0; }
+                        const int32_t x = border(P, P.first_column_free, w.m[l]);
+                        if (better(x, w.m[l], 0, w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = x; w.ci[l] = w.m[l]; w.cj[l] = 0; }
                     }
                 }
                 pa_result r;
-                r.score = cs[l];
-                r.end1 = ci[l];
-                r.end2 = cj[l];
+                r.score = w.cs[l];
+                r.end1 = w.ci[l];
+                r.end2 = w.cj[l];
                 r.width = V::WIDTH;
                 r.flags = L.rerun ? PA_RESULT_RERUN : 0;
                 r.band_rounds = 0;
-                if (MODE == M_LOCAL && cs[l] <= 0) { r.end1 = 0; r.end2 = 0; }
-                if (clamp16 && (int64_t)cs[l] <= (int64_t)P.floor16 + (int64_t)P.smax * min(m[l], n[l])) {
+                if (MODE == M_LOCAL && w.cs[l] <= 0) { r.end1 = 0; r.end2 = 0; }
+                if (NL == 2 && MODE != M_LOCAL &&
+                    (int64_t)w.cs[l] <= (int64_t)w.floor_true + (int64_t)P.smax * min(w.m[l], w.n[l])) {
                     // a clamp may have reached this result: recompute the pair in s32
                     const uint32_t slot = atomicAdd(L.rerun_count, 1u);
-                    L.rerun_list[slot] = id[l];
+                    L.rerun_list[slot] = w.id[l];
                     continue;
                 }
-                L.out[id[l]] = r;
+                L.out[w.id[l]] = r;
             }
         }
         __syncwarp(gmask);

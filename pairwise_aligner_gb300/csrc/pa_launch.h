@@ -1,0 +1,15 @@
+// pa_launch.h -- host-side entry points of the DP kernel instantiations.
+// Each kernel variant lives in its own translation unit (pa_kern_v*.cu) so that
+// the library builds in parallel.
+#pragma once
+#include "pa_common.cuh"
+
+namespace pa {
+
+// lanes16: s16x2 lanes (else s32); gen: byte-compare scoring; mode: Mode.
+// Returns the resident blocks per SM of the selected kernel.
+int dp_occupancy(int variant, bool lanes16, bool gen, int mode);
+void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStream_t stream, const DpLaunch &L,
+               const DpParams &P);
+
+}  // namespace pa
