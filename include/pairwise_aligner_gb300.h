@@ -89,6 +89,8 @@ typedef struct pa_result {
 #define PA_RESULT_BANDED     0x02u  /* certified banded result                              */
 #define PA_RESULT_FULL_DP    0x04u  /* band fell back to the full DP                        */
 #define PA_RESULT_TRIVIAL    0x08u  /* an empty sequence: answered without a DP             */
+#define PA_RESULT_OVERFLOW   0x10u  /* pa_align_batch_device_static only: the pair's scores
+                                       could exceed int32; score is INT32_MIN                */
 
 /* Context options; zero-initialised means defaults. */
 typedef struct pa_options {
@@ -139,6 +141,30 @@ pa_status pa_align_batch_device(pa_ctx *ctx, const pa_config *config,
                                 const uint8_t *d_seq1, const uint64_t *d_off1, uint64_t seq1_bytes,
                                 const uint8_t *d_seq2, const uint64_t *d_off2, uint64_t seq2_bytes,
                                 uint64_t n_pairs, pa_result *d_out, void *stream, pa_stats *stats);
+
+/* Same alignment with NO allocation of any kind; this entry point has no
+ * counterpart in the reference.  It is for callers that cannot allocate device
+ * memory when they align: runtimes whose own allocator must own every byte,
+ * code that runs while a CUDA graph is captured (cudaMalloc is not allowed
+ * there), or latency-critical paths that must not stall on an allocation.
+ * No context is needed: the caller passes device inputs and the device output
+ * (n_pairs pa_result) and a stream (NULL = the legacy default stream).
+ *  - Scratch: the pass-boundary rows live in a file-scope device array of
+ *    4,194,304 cells (32 MiB) that every GPU loading the library holds until
+ *    the process exits.  seq1_bytes + n_pairs must not exceed 4,194,304,
+ *    else PA_ERR_TOO_LARGE is returned and nothing is launched.
+ *  - The first call on a device looks up that array's device address
+ *    (cudaGetSymbolAddress) with the device current; make that first call
+ *    before any stream capture.
+ *  - All calls share the array: calls whose work overlaps on the GPU (other
+ *    streams, other host threads) race.  Serialise them.
+ *  - Arithmetic is s32 with raw byte comparison, pairs in input order; a pair
+ *    whose scores could exceed int32 gets INT32_MIN and PA_RESULT_OVERFLOW.
+ * Results equal those of pa_align_batch_device except the width field (32). */
+pa_status pa_align_batch_device_static(const pa_config *config,
+                                       const uint8_t *d_seq1, const uint64_t *d_off1, uint64_t seq1_bytes,
+                                       const uint8_t *d_seq2, const uint64_t *d_off2, uint64_t seq2_bytes,
+                                       uint64_t n_pairs, pa_result *d_out, void *stream);
 
 /* One query against many targets (interface/interface_one_to_many_bulk.hpp:47-92):
  * pair k is (query, targets[k]).  Host buffers, synchronous. */

@@ -21,7 +21,7 @@ STATUS = {
     8: "PA_ERR_TOO_LARGE",
 }
 
-RESULT_RERUN, RESULT_BANDED, RESULT_FULL_DP, RESULT_TRIVIAL = 0x01, 0x02, 0x04, 0x08
+RESULT_RERUN, RESULT_BANDED, RESULT_FULL_DP, RESULT_TRIVIAL, RESULT_OVERFLOW = 0x01, 0x02, 0x04, 0x08, 0x10
 
 
 class PaConfig(ctypes.Structure):
@@ -100,6 +100,9 @@ SIGNATURES = {
     "pa_align_batch_device": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
                                ctypes.c_void_p, ctypes.POINTER(PaStats)], ctypes.c_int),
+    "pa_align_batch_device_static": ([ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
+                                      ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "pa_align_one_to_many": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
                               ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(PaStats)],
                              ctypes.c_int),

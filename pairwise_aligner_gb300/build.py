@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libpa_gb300.so")
-SOURCES = ["pa_capi.cu", "pa_kern_v0.cu", "pa_kern_v1.cu", "pa_kern_v2.cu"]
+SOURCES = ["pa_capi.cu", "pa_kern_v0.cu", "pa_kern_v1.cu", "pa_kern_v2.cu", "pa_static.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -47,14 +47,17 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         procs.append(subprocess.Popen(cmd))
-    failed = [p.args for p in procs if p.wait() != 0]
-    if failed:
-        raise RuntimeError(f"nvcc failed: {failed}")
-    tmp = LIB + f".tmp{os.getpid()}"
-    subprocess.check_call([nvcc(), *ARCH, "-shared", "-o", tmp, *objs])
-    os.replace(tmp, LIB)
-    for o in objs:
-        os.remove(o)
+    try:
+        failed = [p.args for p in procs if p.wait() != 0]
+        if failed:
+            raise RuntimeError(f"nvcc failed: {failed}")
+        tmp = LIB + f".tmp{os.getpid()}"
+        subprocess.check_call([nvcc(), *ARCH, "-shared", "-o", tmp, *objs])
+        os.replace(tmp, LIB)
+    finally:
+        for o in objs:
+            if os.path.exists(o):
+                os.remove(o)
     return LIB
 
 
