@@ -1,0 +1,49 @@
+// Runs alignments through the C++20 front-end (include/pairwise_aligner_gb300.hpp)
+// with the reference's rule nesting.  stdin: one case per line,
+//   method open ext match mismatch first_column first_row last_column last_row seq1 seq2
+// (method 0 global / 1 local, end-gap flags 0 penalised / 1 free, "-" = empty sequence).
+// stdout: "score end1 end2" per case, all cases of one configuration aligned in one bulk call.
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "pairwise_aligner_gb300.hpp"
+
+namespace aligner = seqan::pairwise_aligner_gb300;
+
+int main()
+{
+    std::string line;
+    while (std::getline(std::cin, line)) {
+        if (line.empty()) continue;
+        std::istringstream in{line};
+        int method, open, ext, match, mismatch, fc, fr, lc, lr;
+        std::string s1, s2;
+        in >> method >> open >> ext >> match >> mismatch >> fc >> fr >> lc >> lr >> s1 >> s2;
+        if (s1 == "-") s1.clear();
+        if (s2 == "-") s2.clear();
+        using aligner::cfg::end_gap;
+        auto e = [](int f) { return f ? end_gap::free : end_gap::penalised; };
+        std::vector<std::string> seqs1{s1}, seqs2{s2};
+        try {
+            if (method == 1) {
+                auto a = aligner::cfg::configure_aligner(aligner::cfg::score_model_unitary(
+                    aligner::cfg::method_local(aligner::cfg::gap_model_affine(open, ext)), match, mismatch));
+                auto r = a.compute(seqs1, seqs2).front();
+                std::cout << r.score() << ' ' << r.end_position().first << ' ' << r.end_position().second << '\n';
+            } else {
+                auto a = aligner::cfg::configure_aligner(aligner::cfg::score_model_unitary_simd_saturated(
+                    aligner::cfg::method_global(aligner::cfg::gap_model_affine(open, ext),
+                                                aligner::cfg::leading_end_gap{e(fc), e(fr)},
+                                                aligner::cfg::trailing_end_gap{e(lc), e(lr)}),
+                    match, mismatch));
+                auto r = a.compute(s1, s2);
+                std::cout << r.score() << ' ' << r.end_position().first << ' ' << r.end_position().second << '\n';
+            }
+        } catch (std::exception const &ex) {
+            std::cout << "error " << ex.what() << '\n';
+        }
+    }
+    return 0;
+}

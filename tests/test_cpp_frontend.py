@@ -1,0 +1,45 @@
+"""The header-only C++20 front-end (include/pairwise_aligner_gb300.hpp).
+
+CPU: it compiles with the reference-style rule nesting and links against the
+C ABI library.  GPU: the reference's scalar KATs run through it.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+
+import pytest
+
+from conftest import REPO
+
+
+@pytest.fixture(scope="module")
+def runner(built_lib, tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("cpp") / "kat_runner")
+    libdir = os.path.dirname(built_lib)
+    subprocess.check_call(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-Werror",
+                           "-I", os.path.join(REPO, "include"), os.path.join(REPO, "tests", "cpp", "kat_runner.cpp"),
+                           "-L", libdir, "-lpa_gb300", f"-Wl,-rpath,{libdir}", "-o", exe])
+    return exe
+
+
+def test_cpp_frontend_compiles_and_links(runner):
+    assert os.path.exists(runner)
+
+
+def _line(c):
+    e = lambda k: "1" if c[k] == "free" else "0"
+    return " ".join([("1" if c["method"] == "local" else "0"), str(c["gap_open"]), str(c["gap_extension"]),
+                     str(c["match"]), str(c["mismatch"]), e("first_column"), e("first_row"), e("last_column"),
+                     e("last_row"), c["seq1"] or "-", c["seq2"] or "-"])
+
+
+@pytest.mark.gpu
+def test_cpp_frontend_reference_kats(runner, kats):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    out = subprocess.run([runner], input="\n".join(_line(c) for c in kats) + "\n", capture_output=True, text=True,
+                         check=True).stdout.split("\n")
+    for c, line in zip(kats, out):
+        assert int(line.split()[0]) == c["expected_score"], (c["source"], c["name"], line)
