@@ -173,6 +173,30 @@ pa_status pa_align_one_to_many(pa_ctx *ctx, const pa_config *config,
                                const uint8_t *targets, const uint64_t *target_off,
                                uint64_t n_targets, pa_result *out, pa_stats *stats);
 
+/* Kernel choices of a context.  Replaces nothing in the reference (its tile
+ * shapes are compile-time lane widths, simd/simd_base.hpp:28-57).
+ * variant: inner-loop form of the DP (0 three-operand max, 1 short chain,
+ * 2 three-operand with at most 85 registers, 3 branch-free top input with L1
+ * prefetch, 4 as 3 with a two-op vertical-gap chain); group_threads: lanes
+ * per pair group (1..32, power of two).  Index 0 = local, 1 = global. */
+typedef struct pa_tuning {
+    int32_t variant_s16[2];
+    int32_t variant_s32[2];
+    int32_t group_threads_s16[2];
+    int32_t group_threads_s32[2];
+    double best_ms[2];          /* pa_autotune: device time of the chosen candidate        */
+} pa_tuning;
+
+/* Time every (variant, group_threads) candidate on this batch (host buffers,
+ * as pa_align_batch) and keep the fastest for the config's method on this
+ * context; the choice is also written to *out (may be NULL). */
+pa_status pa_autotune(pa_ctx *ctx, const pa_config *config,
+                      const uint8_t *seq1, const uint64_t *off1,
+                      const uint8_t *seq2, const uint64_t *off2,
+                      uint64_t n_pairs, pa_tuning *out);
+pa_status pa_get_tuning(const pa_ctx *ctx, pa_tuning *out);
+pa_status pa_set_tuning(pa_ctx *ctx, const pa_tuning *tuning);
+
 /* Measured whole-chip throughput of the cell-update instruction mix, used as
  * the roofline denominator: packed s16x2 DPX cell updates per second and s32
  * cell updates per second, from a timed in-register microkernel. */

@@ -78,6 +78,16 @@ class PaStats(ctypes.Structure):
     ]
 
 
+class PaTuning(ctypes.Structure):
+    _fields_ = [
+        ("variant_s16", ctypes.c_int32 * 2),
+        ("variant_s32", ctypes.c_int32 * 2),
+        ("group_threads_s16", ctypes.c_int32 * 2),
+        ("group_threads_s32", ctypes.c_int32 * 2),
+        ("best_ms", ctypes.c_double * 2),
+    ]
+
+
 class PaRoofline(ctypes.Structure):
     _fields_ = [
         ("s16x2_cells_per_s", ctypes.c_double),
@@ -107,6 +117,10 @@ SIGNATURES = {
                               ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(PaStats)],
                              ctypes.c_int),
     "pa_measure_roofline": ([_ctxp, ctypes.POINTER(PaRoofline)], ctypes.c_int),
+    "pa_autotune": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                     ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(PaTuning)], ctypes.c_int),
+    "pa_get_tuning": ([_ctxp, ctypes.POINTER(PaTuning)], ctypes.c_int),
+    "pa_set_tuning": ([_ctxp, ctypes.POINTER(PaTuning)], ctypes.c_int),
     "pa_status_string": ([ctypes.c_int], ctypes.c_char_p),
     "pa_last_error": ([_ctxp], ctypes.c_char_p),
     "pa_abi_version": ([], ctypes.c_int),

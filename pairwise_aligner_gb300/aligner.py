@@ -61,6 +61,40 @@ class Context:
         except Exception:
             pass
 
+    # -- kernel choices -------------------------------------------------------
+    def tuning(self) -> dict:
+        t = _lib.PaTuning()
+        _lib.check(self.lib.pa_get_tuning(self.ptr, ctypes.byref(t)), self.ptr)
+        return {name: list(getattr(t, name)) for name, _ in _lib.PaTuning._fields_}
+
+    def set_tuning(self, tuning: dict):
+        t = _lib.PaTuning()
+        for name, _ in _lib.PaTuning._fields_:
+            getattr(t, name)[:] = tuning[name]
+        _lib.check(self.lib.pa_set_tuning(self.ptr, ctypes.byref(t)), self.ptr)
+
+    def autotune(self, c_config, seq1, off1, seq2, off2) -> dict:
+        """Time the kernel candidates on this batch and keep the fastest for its method."""
+        seq1 = np.ascontiguousarray(seq1, dtype=np.uint8)
+        seq2 = np.ascontiguousarray(seq2, dtype=np.uint8)
+        off1 = np.ascontiguousarray(off1, dtype=np.uint64)
+        off2 = np.ascontiguousarray(off2, dtype=np.uint64)
+        t = _lib.PaTuning()
+        _lib.check(self.lib.pa_autotune(self.ptr, ctypes.byref(c_config), seq1.ctypes.data, off1.ctypes.data,
+                                        seq2.ctypes.data, off2.ctypes.data, len(off1) - 1, ctypes.byref(t)),
+                   self.ptr)
+        return {name: list(getattr(t, name)) for name, _ in _lib.PaTuning._fields_}
+
+    def save_tuning(self, path: str):
+        import json
+        with open(path, "w") as f:
+            json.dump(self.tuning(), f, indent=1)
+
+    def load_tuning(self, path: str):
+        import json
+        with open(path) as f:
+            self.set_tuning(json.load(f))
+
     def roofline(self) -> dict:
         r = _lib.PaRoofline()
         _lib.check(self.lib.pa_measure_roofline(self.ptr, ctypes.byref(r)), self.ptr)

@@ -60,6 +60,8 @@ struct pa_ctx {
     DevBuf in_seq1, in_off1, in_seq2, in_off2, in_out;   // staging for the host-buffer entry points
     int G[3] = {kDefaultG, kDefaultG, kDefaultG};
     int variant[3] = {0, 0, 0};
+    pa_tuning tuning{};           // per method (0 local, 1 global); applied to G/variant per call
+    bool fixed_G = false, fixed_variant = false;
     int grid[3] = {0, 0, 0};
     std::map<GraphKey, cudaGraphExec_t> graphs;
     uint64_t last_launches = 0;
@@ -144,14 +146,20 @@ namespace pa {
 int dp_occupancy_v0(bool lanes16, bool gen, int mode);
 int dp_occupancy_v1(bool lanes16, bool gen, int mode);
 int dp_occupancy_v2(bool lanes16, bool gen, int mode);
+int dp_occupancy_v3(bool lanes16, bool gen, int mode);
+int dp_occupancy_v4(bool lanes16, bool gen, int mode);
 void dp_launch_v0(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v1(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v2(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
+void dp_launch_v3(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
+void dp_launch_v4(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 
 int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
 {
     if (variant == 1) return dp_occupancy_v1(lanes16, gen, mode);
     if (variant == 2) return dp_occupancy_v2(lanes16, gen, mode);
+    if (variant == 3) return dp_occupancy_v3(lanes16, gen, mode);
+    if (variant == 4) return dp_occupancy_v4(lanes16, gen, mode);
     return dp_occupancy_v0(lanes16, gen, mode);
 }
 
@@ -160,6 +168,8 @@ void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStre
 {
     if (variant == 1) dp_launch_v1(lanes16, gen, mode, grid, st, L, P);
     else if (variant == 2) dp_launch_v2(lanes16, gen, mode, grid, st, L, P);
+    else if (variant == 3) dp_launch_v3(lanes16, gen, mode, grid, st, L, P);
+    else if (variant == 4) dp_launch_v4(lanes16, gen, mode, grid, st, L, P);
     else dp_launch_v0(lanes16, gen, mode, grid, st, L, P);
 }
 }  // namespace pa
@@ -169,7 +179,7 @@ namespace {
 // Resident blocks per SM of every DP kernel, queried once outside any stream capture.
 void warm_occupancy()
 {
-    for (int v = 0; v < 3; ++v)
+    for (int v = 0; v < 5; ++v)
         for (int mode = 0; mode < 3; ++mode) {
             dp_occupancy(v, true, false, mode);
             dp_occupancy(v, false, false, mode);
@@ -227,7 +237,11 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
 
     const uint32_t *ranges = (const uint32_t *)c->ranges.p;
     const uint32_t *counts = (const uint32_t *)c->counts.p;
-    PA_CUDA(c, cudaEventRecordWithFlags(c->ev_dp0, st, cudaEventRecordExternal));
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    PA_CUDA(c, cudaStreamIsCapturing(st, &capturing));
+    // inside a capture the record must become a graph node to fire on every replay
+    const unsigned ev_flags = capturing == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
+    PA_CUDA(c, cudaEventRecordWithFlags(c->ev_dp0, st, ev_flags));
     // s16x2 class
     L.begin_ptr = ranges + K_S16; L.count_ptr = counts + K_S16; L.unit_counter = counters + 0; L.G = c->G[K_S16];
     launch_class(c, K_S16, mode, true, false, L, P);
@@ -247,7 +261,7 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
         L.G = c->G[K_S32];
         launch_class(c, K_S32, mode, false, false, L, P);
     }
-    PA_CUDA(c, cudaEventRecordWithFlags(c->ev_dp1, st, cudaEventRecordExternal));
+    PA_CUDA(c, cudaEventRecordWithFlags(c->ev_dp1, st, ev_flags));
     PA_CUDA(c, cudaGetLastError());
     (void)cfg;
     return PA_OK;
@@ -277,6 +291,17 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
                      const uint8_t *s2, const uint64_t *o2, uint64_t b2, uint64_t n_pairs, pa_result *out,
                      pa_stats *stats, bool sync_for_stats)
 {
+    if (cfg) {
+        const int mi = cfg->method == PA_METHOD_LOCAL ? 0 : 1;
+        if (!c->fixed_variant) {
+            c->variant[K_S16] = c->tuning.variant_s16[mi];
+            c->variant[K_S32] = c->variant[K_GEN] = c->tuning.variant_s32[mi];
+        }
+        if (!c->fixed_G) {
+            c->G[K_S16] = c->tuning.group_threads_s16[mi];
+            c->G[K_S32] = c->G[K_GEN] = c->tuning.group_threads_s32[mi];
+        }
+    }
     DpParams P;
     ClassCfg C;
     pa_status s = check_config(c, cfg, P, C);
@@ -434,14 +459,20 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
         delete c;
         return PA_ERR_CUDA;
     }
+    // defaults measured on GB300 (262,144 pairs of 64..512 bp): local s16x2 is fastest with
+    // variant 3, global with variant 4; 8 lanes per group
+    c->tuning = pa_tuning{{3, 4}, {0, 4}, {8, 8}, {8, 8}, {0.0, 0.0}};
     if (c->opt.group_threads) {
         int g = c->opt.group_threads;
         if (g < 1 || g > 32 || (g & (g - 1))) { pa_destroy(c); return PA_ERR_INVALID_ARGUMENT; }
         for (int k = 0; k < 3; ++k) c->G[k] = g;
+        c->fixed_G = true;
     }
     if (c->opt.rows_per_thread && c->opt.rows_per_thread != kR) { pa_destroy(c); return PA_ERR_UNSUPPORTED; }
-    if (c->opt.kernel_variant >= 0 && c->opt.kernel_variant <= 2)
+    if (c->opt.kernel_variant >= 0 && c->opt.kernel_variant <= 4) {
         for (int k = 0; k < 3; ++k) c->variant[k] = c->opt.kernel_variant;
+        c->fixed_variant = true;
+    }
     else if (c->opt.kernel_variant != -1) { pa_destroy(c); return PA_ERR_INVALID_ARGUMENT; }
     warm_occupancy();
     *out = c;
@@ -573,6 +604,62 @@ pa_status pa_align_one_to_many(pa_ctx *ctx, const pa_config *config, const uint8
     }
     qo[n_targets] = n_targets * query_len;
     return pa_align_batch(ctx, config, q.data(), qo.data(), targets, target_off, n_targets, out, stats);
+}
+
+pa_status pa_get_tuning(const pa_ctx *ctx, pa_tuning *out)
+{
+    if (!ctx || !out) return PA_ERR_INVALID_ARGUMENT;
+    *out = ctx->tuning;
+    return PA_OK;
+}
+
+static bool valid_G(int g) { return g >= 1 && g <= 32 && (g & (g - 1)) == 0; }
+static bool valid_variant(int v) { return v >= 0 && v <= 4; }
+
+pa_status pa_set_tuning(pa_ctx *ctx, const pa_tuning *t)
+{
+    if (!ctx || !t) return PA_ERR_INVALID_ARGUMENT;
+    for (int m = 0; m < 2; ++m)
+        if (!valid_variant(t->variant_s16[m]) || !valid_variant(t->variant_s32[m]) || !valid_G(t->group_threads_s16[m]) ||
+            !valid_G(t->group_threads_s32[m]))
+            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "tuning: variant must be 0..4 and group_threads 1..32, power of two");
+    ctx->tuning = *t;
+    ctx->fixed_G = ctx->fixed_variant = false;
+    return PA_OK;
+}
+
+pa_status pa_autotune(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1, const uint64_t *off1,
+                      const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, pa_tuning *out)
+{
+    if (!ctx || !config) return PA_ERR_INVALID_ARGUMENT;
+    const int mi = config->method == PA_METHOD_LOCAL ? 0 : 1;
+    const pa_tuning saved = ctx->tuning;
+    const bool fg = ctx->fixed_G, fv = ctx->fixed_variant;
+    ctx->fixed_G = ctx->fixed_variant = false;
+    std::vector<pa_result> res(std::max<uint64_t>(n_pairs, 1));
+    double best = 1e300;
+    pa_tuning choice = saved;
+    static const int kVariants[] = {0, 1, 3, 4};
+    static const int kGroups[] = {4, 8, 16};
+    for (int v : kVariants)
+        for (int g : kGroups) {
+            pa_tuning t = saved;
+            t.variant_s16[mi] = t.variant_s32[mi] = v;
+            t.group_threads_s16[mi] = t.group_threads_s32[mi] = g;
+            ctx->tuning = t;
+            double ms = 1e300;
+            for (int rep = 0; rep < 3; ++rep) {                 // first run captures the graph
+                pa_stats st;
+                pa_status s = pa_align_batch(ctx, config, seq1, off1, seq2, off2, n_pairs, res.data(), &st);
+                if (s) { ctx->tuning = saved; ctx->fixed_G = fg; ctx->fixed_variant = fv; return s; }
+                if (rep > 0) ms = std::min(ms, st.dp_ms);
+            }
+            if (ms < best) { best = ms; choice = t; }
+        }
+    choice.best_ms[mi] = best;
+    ctx->tuning = choice;
+    if (out) *out = choice;
+    return PA_OK;
 }
 
 pa_status pa_measure_roofline(pa_ctx *ctx, pa_roofline *out)

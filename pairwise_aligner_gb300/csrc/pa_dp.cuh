@@ -149,6 +149,8 @@ __device__ __forceinline__ uint32_t stored(const GroupWork &w, int32_t true_valu
     return V::splat(x);
 }
 
+// VAR bit 0: short-chain form of the vertical gap; bit 2: branch-free top input for
+// thread 0 and an L1 prefetch of the score tables eight columns ahead.
 template <class V, int R, int RA, int MODE, bool GEN, int VAR>
 __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, GroupWork &w, int p, int t, int G,
                                          unsigned gmask, uint4 *snap)
@@ -158,6 +160,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
     const uint32_t GOEA = V::cabs(P.gap_open + P.gap_ext);
     const uint32_t EXTA = V::cabs(P.gap_ext);
     const uint32_t CLAMP = w.CLAMP;
+    const uint32_t CLAMPG = V::LANES == 2 ? V::subc(CLAMP, GOEA) : (uint32_t)max((int)CLAMP, INT32_MIN + 65536) - GOEA;
 
     uint32_t H[RA], Fr[RA], Sel[RA];
 #pragma unroll
@@ -204,11 +207,27 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
     };
     Cell nbuf = Cell{0u, 0u};                        // thread 0, pass > 0: next boundary cell
     if (t == 0 && p > 0) nbuf = w.buf[1];
+    constexpr bool TUNED = (VAR & 4) != 0;
+    const bool first_thread = t == 0;
+    const bool top_border = first_thread && p == 0;
+    const bool top_buffer = first_thread && p > 0;
     auto step = [&](int32_t i, bool active) {
         uint32_t upH = __shfl_up_sync(gmask, outH, 1, G);
         uint32_t upE = __shfl_up_sync(gmask, outE, 1, G);
         if (!active) return;
-        if (t == 0) {
+        if (TUNED) {
+            // every lane computes the border candidate; thread 0 selects it (no divergence)
+            const uint32_t nt = V::max2(V::subc(topH, i == 1 ? step1 : stepn), CLAMP);
+            topH = top_border ? nt : topH;
+            const Cell c = nbuf;
+            if (top_buffer && i < ms) nbuf = w.buf[i + 1];
+            upH = top_border ? nt : (top_buffer ? c.h : upH);
+            upE = top_border ? V::subc(nt, GOEA) : (top_buffer ? c.e : upE);
+            if (!GEN && i + 8 <= ms) {
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(w.qt[0] + min(i + 7, w.m[0])));
+                if (NL == 2) asm volatile("prefetch.global.L1 [%0];" ::"l"(w.qt[1] + min(i + 7, w.m[1])));
+            }
+        } else if (t == 0) {
             if (p == 0) {
                 topH = V::max2(V::subc(topH, i == 1 ? step1 : stepn), CLAMP);
                 upH = topH;
@@ -233,7 +252,14 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             }
             const uint32_t tt = V::addmax(diag, sc, Fr[k]);
             diag = H[k];
-            if (VAR == 0) {
+            if ((VAR & 8) != 0) {
+                // vgap' = max(vgap + ext, t + open + ext, clamp + open + ext): the H term of the
+                // vertical gap is dominated, so the serial chain is one IADD and one VIMAX3
+                const uint32_t h = V::hmax(tt, Ed, CLAMP);
+                H[k] = h;
+                Fr[k] = V::max2(V::subc(Fr[k], EXTA), V::subc(h, GOEA));
+                Ed = V::max3(V::subc(Ed, EXTA), V::subc(tt, GOEA), CLAMPG);
+            } else if ((VAR & 1) == 0) {
                 const uint32_t h = V::hmax(tt, Ed, CLAMP);
                 H[k] = h;
                 const uint32_t hoe = V::subc(h, GOEA);

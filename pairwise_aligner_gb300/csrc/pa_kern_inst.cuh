@@ -1,12 +1,14 @@
 // pa_kern_inst.cuh -- per-variant launcher body, included once per pa_kern_v*.cu
 // with PA_VARIANT defined.  Variant 0: three-operand H max, 2 blocks/SM;
-// 1: short-chain H, 2 blocks/SM; 2: as 0 with at most 85 registers (3 blocks/SM).
+// 1: short-chain H, 2 blocks/SM; 2: as 0 with at most 85 registers (3 blocks/SM);
+// 3: as 0 with a branch-free top input and L1 prefetch of the score tables;
+// 4: as 3 with the two-op vertical-gap chain.
 #ifndef PA_VARIANT
 #error "define PA_VARIANT"
 #endif
 
 namespace {
-constexpr int kVarMath = PA_VARIANT == 1 ? 1 : 0;
+constexpr int kVarMath = PA_VARIANT == 1 ? 1 : (PA_VARIANT == 3 ? 4 : (PA_VARIANT == 4 ? 12 : 0));
 constexpr int kVarMinB = PA_VARIANT == 2 ? 3 : 2;
 constexpr int kRows = 16;
 

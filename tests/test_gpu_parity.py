@@ -75,6 +75,21 @@ def test_group_sizes_config2_sample(pa, oracle, group_threads):
     _check(oracle, d, res)
 
 
+@pytest.mark.parametrize("local", [True, False])
+@pytest.mark.parametrize("use_graphs,variant", [(-1, 0), (1, 1), (-1, 2), (1, 3), (-1, 4)])
+def test_launch_paths_and_variants(pa, oracle, use_graphs, variant, local):
+    """Direct launches and graph replays, every inner-loop variant: same results, stats filled."""
+    from pairwise_aligner_gb300 import workloads as W
+    d = W.config2(seed=13, n_pairs=3000)
+    if not local:
+        d.update(local=False, last_row_free=variant % 2 == 1)
+    al = _aligner_for(pa, d, use_graphs=use_graphs, kernel_variant=variant)
+    for _ in range(2):
+        res = al.compute_arrays(d["seq1"], d["off1"], d["seq2"], d["off2"])
+        _check(oracle, d, res)
+        assert al.last_stats["device_ms"] > 0 and al.last_stats["dp_ms"] > 0
+
+
 def test_config1_full(pa, oracle):
     from pairwise_aligner_gb300 import workloads as W
     d = W.config1()
@@ -208,3 +223,22 @@ def test_invalid_arguments(pa):
                       first_row_free=0, last_column_free=0, last_row_free=0))
     with pytest.raises(ValueError):
         ok.compute_arrays(*pa.pack(["A", "C"]), *pa.pack(["A"]))
+
+
+def test_autotune_keeps_results_exact(pa, oracle, tmp_path):
+    from pairwise_aligner_gb300 import workloads as W
+    d = W.config2(seed=17, n_pairs=2048)
+    al = _aligner_for(pa, d)
+    ctx = al.context
+    before = ctx.tuning()
+    t = ctx.autotune(al.c_config(), d["seq1"], d["off1"], d["seq2"], d["off2"])
+    assert t["variant_s16"][0] in (0, 1, 3, 4) and t["group_threads_s16"][0] in (4, 8, 16)
+    assert t["best_ms"][0] > 0
+    assert t["variant_s16"][1] == before["variant_s16"][1]          # the other method is untouched
+    res = al.compute_arrays(d["seq1"], d["off1"], d["seq2"], d["off2"])
+    _check(oracle, d, res)
+    path = str(tmp_path / "tuning.json")
+    ctx.save_tuning(path)
+    fresh = pa.Context(0)
+    fresh.load_tuning(path)
+    assert fresh.tuning()["variant_s16"] == t["variant_s16"]
