@@ -67,7 +67,10 @@ typedef struct pa_config {
     uint8_t last_column_free;   /* the result may end anywhere in column n                */
     uint8_t last_row_free;      /* the result may end anywhere in row m                   */
     int32_t width_hint;         /* 0 auto (s16x2 then s32), 16, or 32                     */
-    int32_t band_mode;          /* 0: plain full DP.  1: learned band + certificate       */
+    int32_t band_mode;          /* 0: plain full DP.  Global alignment with penalised end
+                                   gaps only: 1 learned band (pa_set_band_model), 2 the
+                                   straight-line band; both with certificate, doubling and
+                                   the full DP as fallback, so scores are unchanged      */
 } pa_config;
 
 /* Per-pair result (16 bytes).  score mirrors aligner_result::score()
@@ -115,6 +118,10 @@ typedef struct pa_stats {
     uint64_t kernel_launches;   /* kernels this call launched                             */
     double   device_ms;         /* device time of the whole call (CUDA events)            */
     double   dp_ms;             /* device time of the DP kernels alone                    */
+    uint64_t pairs_banded;      /* band mode: results accepted by the certificate         */
+    uint64_t pairs_full_dp;     /* band mode: results of the full-DP fallback             */
+    uint64_t band_cells;        /* band mode: cells the banded DP computed (all rounds)   */
+    uint64_t band_rounds;       /* band mode: band widths tried                           */
 } pa_stats;
 
 typedef struct pa_ctx pa_ctx;
@@ -172,6 +179,77 @@ pa_status pa_align_one_to_many(pa_ctx *ctx, const pa_config *config,
                                const uint8_t *query, uint64_t query_len,
                                const uint8_t *targets, const uint64_t *target_off,
                                uint64_t n_targets, pa_result *out, pa_stats *stats);
+
+/* Band-predictor training labels (global alignment only; no counterpart in the
+ * reference): for every pair the diagonal j - i_c of the optimal path at the 8
+ * checkpoint columns i_c = c*m/9 (c = 1..8) of sequence1, from a forward and a
+ * reverse full DP on the GPU (the argmax over j of the best score through
+ * (i_c, j); ties to the smallest j).  Host buffers; labels has 8 * n_pairs
+ * entries (0 for pairs with m < 9 or an empty sequence2). */
+pa_status pa_band_labels(pa_ctx *ctx, const pa_config *config,
+                         const uint8_t *seq1, const uint64_t *off1,
+                         const uint8_t *seq2, const uint64_t *off2,
+                         uint64_t n_pairs, int32_t *labels);
+
+/* Band predictor building blocks (device pointers, asynchronous on `stream`;
+ * no counterpart in the reference).  pa_band_features_device writes 130 floats
+ * per pair: the 128-bin histogram of diagonal offsets j - i of shared 12-mers
+ * (bins over [-m, n], divided by the number of sequence1 12-mers), m/1024, n/1024.
+ * The pa_mlp_* calls are the training and inference kernels of the BF16 MLP
+ * 130 -> 256 -> 256 -> 9: a BF16 tensor-core GEMM with FP32 accumulation and a
+ * fused bias/ReLU epilogue, the MSE loss gradient, the ReLU derivative, bias
+ * gradients, Adam on FP32 master weights, and FP32 -> BF16 padding. */
+pa_status pa_band_features_device(const uint8_t *d_seq1, const uint64_t *d_off1,
+                                  const uint8_t *d_seq2, const uint64_t *d_off2,
+                                  uint64_t n_pairs, float *d_features, void *stream);
+pa_status pa_mlp_gemm(const void *A, const void *B, float *C32, void *C16, const float *bias,
+                      int M, int N, int K, int lda, int ldb, int ldc, int ta, int tb, int relu,
+                      float beta, void *stream);
+pa_status pa_mlp_mse(const float *out, const float *target, const float *mask, int batch,
+                     void *dout, float *loss_sum, void *stream);
+pa_status pa_mlp_relu_grad(void *dh, const void *h, int n, void *stream);
+pa_status pa_mlp_colsum(const void *d, int batch, int n_cols, float *db, void *stream);
+pa_status pa_mlp_adam(float *w, void *w16, const float *grad, float *m1, float *m2, int n,
+                      float lr, float beta1, float beta2, float eps, int step, float weight_decay,
+                      void *stream);
+pa_status pa_mlp_to_bf16(const float *src, int rows, int cols, int ld_dst, void *dst, void *stream);
+
+/* Band mode (no counterpart in the reference, which has no banded mode).
+ * A pair's band: the centre line through (0, 0), the checkpoints
+ * (i_c, i_c + diag[c]) with i_c = (c + 1) * m / 9, c = 0..7, and (m, n),
+ * widened to also cover the diagonal n - m; the half-width tapers linearly
+ * from w_start at column 0 to w_min at column m.  Every round the banded DP
+ * proves its score or the band doubles; a pair whose band would cover more
+ * than full_frac of its matrix, or that is still open after max_rounds, is
+ * computed by the full DP.  margin scales the learned starting width;
+ * straight_w0 is the starting width of band_mode 2. */
+typedef struct pa_band_options {
+    float margin;               /* default 1.25 */
+    int32_t w_min;              /* default 16   */
+    int32_t straight_w0;        /* default 64   */
+    float full_frac;            /* default 0.5  */
+    int32_t max_rounds;         /* default 6    */
+    int32_t reserved[3];
+} pa_band_options;
+
+pa_status pa_set_band_options(pa_ctx *ctx, const pa_band_options *options);
+pa_status pa_get_band_options(const pa_ctx *ctx, pa_band_options *out);
+
+/* Load the band predictor of band_mode 1: FP32 host arrays of the MLP
+ * 130 -> 256 -> 256 -> 9 in padded row-major layout, w1 144 x 256 (rows
+ * 130..143 unused), b1 256, w2 256 x 256, b2 256, w3 256 x 16 (columns 9..15
+ * unused), b3 16.  Outputs 0..7 are the checkpoint diagonals divided by
+ * (m + n) / 4, output 8 is log2(1 + smax (m + n) - 2 score) / 16. */
+pa_status pa_set_band_model(pa_ctx *ctx, const float *w1, const float *b1, const float *w2,
+                            const float *b2, const float *w3, const float *b3);
+
+/* Band mode with caller-given bands: 10 int32 per pair (diag[8], w_start,
+ * w_min), otherwise as pa_align_batch (config->band_mode is ignored). */
+pa_status pa_align_batch_banded(pa_ctx *ctx, const pa_config *config,
+                                const uint8_t *seq1, const uint64_t *off1,
+                                const uint8_t *seq2, const uint64_t *off2,
+                                uint64_t n_pairs, const int32_t *bands,
+                                pa_result *out, pa_stats *stats);
 
 /* Kernel choices of a context.  Replaces nothing in the reference (its tile
  * shapes are compile-time lane widths, simd/simd_base.hpp:28-57).

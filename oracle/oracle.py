@@ -63,6 +63,9 @@ def lib():
         L.pa_oracle_align_batch.argtypes = [ctypes.POINTER(OracleCfg), u8p, u64p, u8p, u64p, ctypes.c_uint64,
                                             i64p, i64p, i64p, ctypes.c_int]
         L.pa_oracle_align_batch.restype = ctypes.c_int
+        L.pa_oracle_row.argtypes = [ctypes.POINTER(OracleCfg), u8p, ctypes.c_uint64, u8p, ctypes.c_uint64,
+                                    ctypes.c_uint64, i64p]
+        L.pa_oracle_row.restype = ctypes.c_int
         L.pa_oracle_simd_batch.argtypes = [ctypes.POINTER(OracleCfg), u8p, u64p, u8p, u64p, ctypes.c_uint64,
                                            i32p, ctypes.c_int]
         L.pa_oracle_simd_batch.restype = ctypes.c_int
@@ -133,3 +136,33 @@ def simd_batch(cfg: OracleCfg, s1, off1, s2, off2, nthreads: int | None = None) 
     if rc:
         raise RuntimeError(f"pa_oracle_simd_batch failed: {rc}")
     return scores[:n]
+
+
+def row(cfg: OracleCfg, s1: bytes, s2: bytes, r: int) -> np.ndarray:
+    """H(r, 0..n) of the global recurrence."""
+    a = np.frombuffer(bytes(s1), dtype=np.uint8) if len(s1) else np.zeros(1, np.uint8)
+    b = np.frombuffer(bytes(s2), dtype=np.uint8) if len(s2) else np.zeros(1, np.uint8)
+    out = np.empty(len(s2) + 1, np.int64)
+    rc = lib().pa_oracle_row(ctypes.byref(cfg), _ptr(a, ctypes.c_uint8), len(s1), _ptr(b, ctypes.c_uint8), len(s2),
+                             r, _ptr(out, ctypes.c_int64))
+    if rc:
+        raise RuntimeError(f"pa_oracle_row failed: {rc}")
+    return out
+
+
+def band_labels(cfg: OracleCfg, s1: bytes, s2: bytes) -> list[int]:
+    """The 8 checkpoint diagonals of the optimal global path, as the GPU labeller defines them:
+    checkpoint rows r_c = (c+1)*m//9; label = argmax_j (H(r_c, j) + H_rev(m - r_c, n - j)) - r_c,
+    j in 0..n-1, smallest j on ties."""
+    m, n = len(s1), len(s2)
+    if m < 9 or n == 0:
+        return [0] * 8
+    rs1, rs2 = bytes(s1)[::-1], bytes(s2)[::-1]
+    out = []
+    for c in range(8):
+        r = (c + 1) * m // 9
+        hf = row(cfg, s1, s2, r)
+        hr = row(cfg, rs1, rs2, m - r)
+        tot = hf[:n] + hr[n - np.arange(n)]
+        out.append(int(np.argmax(tot)) - r)
+    return out

@@ -157,6 +157,36 @@ int pa_oracle_align(const pa_oracle_cfg *c, const uint8_t *s1, uint64_t m, const
     return PA_ORACLE_OK;
 }
 
+/* H(row, 0..n) of the global recurrence (the scalar DP above stopped after
+ * `row` rows of sequence1); out has n + 1 entries.  Used to check the band
+ * labels: the label of checkpoint row r is argmax_j H(r, j) + H'(m - r, n - j)
+ * with H' the same DP on both sequences reversed. */
+int pa_oracle_row(const pa_oracle_cfg *c, const uint8_t *s1, uint64_t m, const uint8_t *s2, uint64_t n,
+                  uint64_t row, int64_t *out)
+{
+    if (!c || !out || row > m || c->local) return PA_ORACLE_EINVAL;
+    const int64_t goe = (int64_t)c->gap_open + c->gap_extension, ext = c->gap_extension;
+    int64_t *vgap = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
+    if (!vgap) return PA_ORACLE_ENOMEM;
+    for (uint64_t j = 0; j <= n; ++j) border_cell(c, c->first_row_free, j, &out[j], &vgap[j]);
+    for (uint64_t i = 1; i <= row; ++i) {
+        int64_t hc, hgap;
+        border_cell(c, c->first_column_free, i, &hc, &hgap);
+        int64_t diag = out[0];
+        out[0] = hc;
+        for (uint64_t j = 1; j <= n; ++j) {
+            int64_t h = max64(max64(diag + ((s1[i - 1] == s2[j - 1]) ? c->match : c->mismatch), vgap[j]), hgap);
+            diag = out[j];
+            out[j] = h;
+            int64_t hoe = h + goe;
+            vgap[j] = max64(vgap[j] + ext, hoe);
+            hgap = max64(hgap + ext, hoe);
+        }
+    }
+    free(vgap);
+    return PA_ORACLE_OK;
+}
+
 /* ------------------------------------------------------------------------- */
 /* batch driver over (bytes, offsets) -- the same layout the C-ABI takes       */
 /* ------------------------------------------------------------------------- */

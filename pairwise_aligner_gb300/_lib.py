@@ -75,6 +75,21 @@ class PaStats(ctypes.Structure):
         ("kernel_launches", ctypes.c_uint64),
         ("device_ms", ctypes.c_double),
         ("dp_ms", ctypes.c_double),
+        ("pairs_banded", ctypes.c_uint64),
+        ("pairs_full_dp", ctypes.c_uint64),
+        ("band_cells", ctypes.c_uint64),
+        ("band_rounds", ctypes.c_uint64),
+    ]
+
+
+class PaBandOptions(ctypes.Structure):
+    _fields_ = [
+        ("margin", ctypes.c_float),
+        ("w_min", ctypes.c_int32),
+        ("straight_w0", ctypes.c_int32),
+        ("full_frac", ctypes.c_float),
+        ("max_rounds", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
     ]
 
 
@@ -119,6 +134,25 @@ SIGNATURES = {
     "pa_measure_roofline": ([_ctxp, ctypes.POINTER(PaRoofline)], ctypes.c_int),
     "pa_autotune": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                      ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(PaTuning)], ctypes.c_int),
+    "pa_band_labels": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                        ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p], ctypes.c_int),
+    "pa_band_features_device": ([ctypes.c_void_p] * 4 + [ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p],
+                                 ctypes.c_int),
+    "pa_mlp_gemm": ([ctypes.c_void_p] * 5 + [ctypes.c_int] * 9 + [ctypes.c_float, ctypes.c_void_p], ctypes.c_int),
+    "pa_mlp_mse": ([ctypes.c_void_p] * 3 + [ctypes.c_int] + [ctypes.c_void_p] * 3, ctypes.c_int),
+    "pa_mlp_relu_grad": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
+    "pa_mlp_colsum": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "pa_mlp_adam": ([ctypes.c_void_p] * 5 + [ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                              ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_void_p],
+                    ctypes.c_int),
+    "pa_mlp_to_bf16": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
+                       ctypes.c_int),
+    "pa_set_band_options": ([_ctxp, ctypes.POINTER(PaBandOptions)], ctypes.c_int),
+    "pa_get_band_options": ([_ctxp, ctypes.POINTER(PaBandOptions)], ctypes.c_int),
+    "pa_set_band_model": ([_ctxp] + [ctypes.c_void_p] * 6, ctypes.c_int),
+    "pa_align_batch_banded": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                               ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                               ctypes.POINTER(PaStats)], ctypes.c_int),
     "pa_get_tuning": ([_ctxp, ctypes.POINTER(PaTuning)], ctypes.c_int),
     "pa_set_tuning": ([_ctxp, ctypes.POINTER(PaTuning)], ctypes.c_int),
     "pa_status_string": ([ctypes.c_int], ctypes.c_char_p),

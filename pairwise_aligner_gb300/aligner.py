@@ -61,6 +61,31 @@ class Context:
         except Exception:
             pass
 
+    # -- band mode ----------------------------------------------------------------
+    def band_options(self) -> dict:
+        o = _lib.PaBandOptions()
+        _lib.check(self.lib.pa_get_band_options(self.ptr, ctypes.byref(o)), self.ptr)
+        return {name: getattr(o, name) for name, _ in _lib.PaBandOptions._fields_ if name != "reserved"}
+
+    def set_band_options(self, **kw):
+        o = _lib.PaBandOptions()
+        _lib.check(self.lib.pa_get_band_options(self.ptr, ctypes.byref(o)), self.ptr)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        _lib.check(self.lib.pa_set_band_options(self.ptr, ctypes.byref(o)), self.ptr)
+
+    def set_band_model(self, state: dict):
+        """Load the band predictor (FP32 arrays W1 144x256, b1, W2 256x256, b2, W3 256x16, b3 16)."""
+        shapes = {"W1": (144, 256), "b1": (256,), "W2": (256, 256), "b2": (256,), "W3": (256, 16), "b3": (16,)}
+        arrs = []
+        for k, shp in shapes.items():
+            a = np.ascontiguousarray(state[k], dtype=np.float32)
+            if a.shape != shp:
+                raise ValueError(f"{k} must have shape {shp}, got {a.shape}")
+            arrs.append(a)
+        _lib.check(self.lib.pa_set_band_model(self.ptr, *[a.ctypes.data for a in arrs]), self.ptr)
+        self._band_model = arrs          # keep the host copies alive with the context
+
     # -- kernel choices -------------------------------------------------------
     def tuning(self) -> dict:
         t = _lib.PaTuning()
@@ -189,6 +214,26 @@ class Aligner:
         _lib.check(rc, ctx.ptr)
         if stats:
             self.last_stats = self._stats_dict(st)
+        return out[:n]
+
+    def compute_banded(self, seq1: np.ndarray, off1: np.ndarray, seq2: np.ndarray, off2: np.ndarray,
+                       bands: np.ndarray) -> np.ndarray:
+        """Band mode with caller-given bands: (n_pairs, 10) int32 rows diag[8], w_start, w_min."""
+        n = len(off1) - 1
+        seq1 = np.ascontiguousarray(seq1, dtype=np.uint8)
+        seq2 = np.ascontiguousarray(seq2, dtype=np.uint8)
+        off1 = np.ascontiguousarray(off1, dtype=np.uint64)
+        off2 = np.ascontiguousarray(off2, dtype=np.uint64)
+        bands = np.ascontiguousarray(bands, dtype=np.int32).reshape(n, 10)
+        out = np.zeros(max(n, 1), dtype=RESULT_DTYPE)
+        st = _lib.PaStats()
+        ctx = self.context
+        cfg = self.c_config()
+        rc = ctx.lib.pa_align_batch_banded(ctx.ptr, ctypes.byref(cfg), seq1.ctypes.data, off1.ctypes.data,
+                                           seq2.ctypes.data, off2.ctypes.data, n, bands.ctypes.data, out.ctypes.data,
+                                           ctypes.byref(st))
+        _lib.check(rc, ctx.ptr)
+        self.last_stats = self._stats_dict(st)
         return out[:n]
 
     def compute_device(self, seq1, off1, seq2, off2, out, stream=None, stats: bool = False):

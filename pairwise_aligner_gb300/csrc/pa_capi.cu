@@ -65,6 +65,12 @@ struct pa_ctx {
     int grid[3] = {0, 0, 0};
     std::map<GraphKey, cudaGraphExec_t> graphs;
     uint64_t last_launches = 0;
+    // band mode
+    pa_band_options band_opt{1.25f, 16, 64, 0.5f, 6, {0, 0, 0}};
+    DevBuf band_spec, band_win, band_code, band_bsum, band_ctr, band_in;
+    DevBuf band_list[8];
+    DevBuf mlp_w[6], mlp_feat, mlp_x, mlp_h1, mlp_h2, mlp_out;
+    bool has_model = false;
 };
 
 namespace {
@@ -111,8 +117,8 @@ pa_status check_config(pa_ctx *c, const pa_config *cfg, DpParams &P, ClassCfg &C
         return fail(c, PA_ERR_UNSUPPORTED, "positive gap scores are not supported");
     if (cfg->width_hint != 0 && cfg->width_hint != 16 && cfg->width_hint != 32)
         return fail(c, PA_ERR_INVALID_ARGUMENT, "width_hint must be 0, 16 or 32");
-    if (cfg->band_mode != 0 && cfg->band_mode != 1)
-        return fail(c, PA_ERR_INVALID_ARGUMENT, "band_mode must be 0 or 1");
+    if (cfg->band_mode < 0 || cfg->band_mode > 2)
+        return fail(c, PA_ERR_INVALID_ARGUMENT, "band_mode must be 0, 1 or 2");
     const bool local = cfg->method == PA_METHOD_LOCAL;
     std::memset(&P, 0, sizeof(P));
     P.match = cfg->match;
@@ -163,6 +169,22 @@ int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
     return dp_occupancy_v0(lanes16, gen, mode);
 }
 
+void band_labels_launch(bool reverse, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
+int band_labels_occupancy();
+int band_dp_occupancy(bool lanes16);
+void band_dp_launch(bool lanes16, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
+void band_windows_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, const uint32_t *list,
+                         uint32_t count, const BandSpec *spec, int32_t rows, int shift, float full_frac, int2 *win,
+                         uint8_t *code);
+void band_decode_launch(cudaStream_t st, const float *out, const uint64_t *off1, const uint64_t *off2,
+                        uint64_t n_pairs, const DpParams &P, float margin, int32_t w_min, BandSpec *spec);
+void band_straight_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, uint64_t n_pairs,
+                          int32_t w_start, int32_t w_min, BandSpec *spec);
+void band_from_ints_launch(cudaStream_t st, const int32_t *in, uint64_t n_pairs, BandSpec *spec);
+void compact_launch(cudaStream_t st, const uint32_t *list, const uint8_t *code, uint32_t count, uint8_t sel,
+                    uint32_t *block_sum, uint32_t *out, uint32_t *total);
+void mark_full_launch(cudaStream_t st, pa_result *out, uint64_t n_pairs);
+
 void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStream_t st, const DpLaunch &L,
                const DpParams &P)
 {
@@ -197,19 +219,17 @@ void launch_class(pa_ctx *c, int slot, int mode, bool lanes16, bool gen, const D
     c->last_launches++;
 }
 
-// Everything between inputs-on-device and results-on-device; no host sync.
-pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const ClassCfg &C, const uint8_t *s1,
-                  const uint64_t *o1, uint64_t b1, const uint8_t *s2, const uint64_t *o2, pa_result *out,
-                  uint64_t n_pairs)
+// Classify, bucket and sort the pairs (steps 1-3); no host sync.
+pa_status enqueue_prep(pa_ctx *c, const DpParams &P, const ClassCfg &C, const uint8_t *s1, const uint64_t *o1,
+                       const uint8_t *s2, const uint64_t *o2, pa_result *out, uint64_t n_pairs)
 {
     cudaStream_t st = c->stream;
-    uint32_t *counters = (uint32_t *)c->counters.p;   // [0..3] unit queues, [4] rerun count, [5] zero
     PA_CUDA(c, cudaMemsetAsync(c->hist.p, 0, sizeof(uint32_t) * kBuckets, st));
     PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, st));
     PA_CUDA(c, cudaMemsetAsync(c->pstats.p, 0, sizeof(PrepStats), st));
-    int cls_blocks = (int)std::min<uint64_t>((n_pairs * 32 + kBlock - 1) / kBlock, (uint64_t)c->sm_count * 64);
+    int cls_blocks = (int)std::min<uint64_t>((n_pairs * 32 + 127) / 128, (uint64_t)c->sm_count * 128);
     if (cls_blocks < 1) cls_blocks = 1;
-    k_classify<<<cls_blocks, kBlock, 0, st>>>(s1, o1, s2, o2, n_pairs, P, C, (uint32_t *)c->keys.p,
+    k_classify<<<cls_blocks, 128, 0, st>>>(s1, o1, s2, o2, n_pairs, P, C, (uint32_t *)c->keys.p,
                                               (uint32_t *)c->hist.p, (uint32_t *)c->qtab.p, out,
                                               (PrepStats *)c->pstats.p);
     k_scan_blocks<<<kBuckets / 1024, 1024, 0, st>>>((uint32_t *)c->hist.p, (uint32_t *)c->starts.p,
@@ -222,6 +242,19 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
                                             (uint32_t *)c->order.p, (uint32_t *)c->ranges.p,
                                             (uint32_t *)c->counts.p);
     c->last_launches += 6;
+    PA_CUDA(c, cudaGetLastError());
+    return PA_OK;
+}
+
+// Everything between inputs-on-device and results-on-device; no host sync.
+pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const ClassCfg &C, const uint8_t *s1,
+                  const uint64_t *o1, uint64_t b1, const uint8_t *s2, const uint64_t *o2, pa_result *out,
+                  uint64_t n_pairs)
+{
+    cudaStream_t st = c->stream;
+    uint32_t *counters = (uint32_t *)c->counters.p;   // [0..3] unit queues, [4] rerun count, [5] zero
+    pa_status ps = enqueue_prep(c, P, C, s1, o1, s2, o2, out, n_pairs);
+    if (ps) return ps;
 
     const int mode = P.local ? M_LOCAL : ((P.last_column_free || P.last_row_free) ? M_GLOBAL_FREE : M_GLOBAL);
     DpLaunch L;
@@ -287,21 +320,254 @@ pa_status prepare_buffers(pa_ctx *c, uint64_t n_pairs, uint64_t b1)
     return PA_OK;
 }
 
+void apply_tuning(pa_ctx *c, const pa_config *cfg)
+{
+    if (!cfg) return;
+    const int mi = cfg->method == PA_METHOD_LOCAL ? 0 : 1;
+    if (!c->fixed_variant) {
+        c->variant[K_S16] = c->tuning.variant_s16[mi];
+        c->variant[K_S32] = c->variant[K_GEN] = c->tuning.variant_s32[mi];
+    }
+    if (!c->fixed_G) {
+        c->G[K_S16] = c->tuning.group_threads_s16[mi];
+        c->G[K_S32] = c->G[K_GEN] = c->tuning.group_threads_s32[mi];
+    }
+}
+
+// Band predictor inference on the device: features, MLP, decode to BandSpec.
+pa_status band_predict(pa_ctx *c, const DpParams &P, const uint8_t *s1, const uint64_t *o1, const uint8_t *s2,
+                       const uint64_t *o2, uint64_t np, BandSpec *spec)
+{
+    const uint64_t chunk = std::min<uint64_t>(np, 65536);
+    pa_status s;
+    if ((s = ensure(c, c->mlp_feat, chunk * 130 * 4))) return s;
+    if ((s = ensure(c, c->mlp_x, chunk * 144 * 2))) return s;
+    if ((s = ensure(c, c->mlp_h1, chunk * 256 * 2))) return s;
+    if ((s = ensure(c, c->mlp_h2, chunk * 256 * 2))) return s;
+    if ((s = ensure(c, c->mlp_out, chunk * 16 * 4))) return s;
+    cudaStream_t st = c->stream;
+    float *feat = (float *)c->mlp_feat.p, *out = (float *)c->mlp_out.p;
+    void *x = c->mlp_x.p, *h1 = c->mlp_h1.p, *h2 = c->mlp_h2.p;
+    const float *b1 = (const float *)c->mlp_w[1].p, *b2 = (const float *)c->mlp_w[3].p,
+                *b3 = (const float *)c->mlp_w[5].p;
+    for (uint64_t start = 0; start < np; start += chunk) {
+        const int cnt = (int)std::min<uint64_t>(chunk, np - start);
+        if ((s = pa_band_features_device(s1, o1 + start, s2, o2 + start, cnt, feat, st)) ||
+            (s = pa_mlp_to_bf16(feat, cnt, 130, 144, x, st)) ||
+            (s = pa_mlp_gemm(x, c->mlp_w[0].p, nullptr, h1, b1, cnt, 256, 144, 144, 256, 256, 0, 0, 1, 0.f, st)) ||
+            (s = pa_mlp_gemm(h1, c->mlp_w[2].p, nullptr, h2, b2, cnt, 256, 256, 256, 256, 256, 0, 0, 1, 0.f, st)) ||
+            (s = pa_mlp_gemm(h2, c->mlp_w[4].p, out, nullptr, b3, cnt, 16, 256, 256, 16, 16, 0, 0, 0, 0.f, st)))
+            return fail(c, s, "band predictor launch failed");
+        band_decode_launch(st, out, o1 + start, o2 + start, cnt, P, c->band_opt.margin, c->band_opt.w_min,
+                           spec + start);
+        c->last_launches += 6;
+    }
+    PA_CUDA(c, cudaGetLastError());
+    return PA_OK;
+}
+
+// Band mode (host-synchronous between rounds): classify and sort as the plain
+// path, build every pair's band, then per round and lane width: windows ->
+// (too wide: full DP list) -> banded DP -> certified results, pairs to widen,
+// and s16 results to redo in s32; finally the full DP for what is left.
+pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uint64_t *o1, uint64_t b1,
+                   const uint8_t *s2, const uint64_t *o2, uint64_t b2, uint64_t n_pairs, pa_result *out,
+                   const int32_t *h_bands, pa_stats *stats)
+{
+    apply_tuning(c, cfg);
+    DpParams P;
+    ClassCfg C;
+    pa_status s = check_config(c, cfg, P, C);
+    if (s) return s;
+    if (P.local || P.first_column_free || P.first_row_free || P.last_column_free || P.last_row_free)
+        return fail(c, PA_ERR_UNSUPPORTED, "band mode needs global alignment with penalised end gaps");
+    if (!h_bands && cfg->band_mode == 1 && !c->has_model)
+        return fail(c, PA_ERR_INVALID_ARGUMENT, "band_mode 1 needs a band model (pa_set_band_model)");
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (n_pairs == 0) return PA_OK;
+    if (!s1 || !o1 || !s2 || !o2 || !out) return fail(c, PA_ERR_INVALID_ARGUMENT, "null buffer");
+    if (n_pairs >= (1ull << 31)) return fail(c, PA_ERR_TOO_LARGE, "n_pairs must be < 2^31");
+    if ((s = prepare_buffers(c, n_pairs, b1))) return s;
+    const uint64_t np = n_pairs;
+    const int rows16 = c->G[K_S16] * kR, rows32 = c->G[K_S32] * kR;
+    if ((s = ensure(c, c->band_spec, np * sizeof(BandSpec)))) return s;
+    if ((s = ensure(c, c->band_win, (b2 / std::min(rows16, rows32) + np + 1) * sizeof(int2)))) return s;
+    if ((s = ensure(c, c->band_code, np))) return s;
+    if ((s = ensure(c, c->band_bsum, (np / 1024 + 2) * 4))) return s;
+    if ((s = ensure(c, c->band_ctr, 256))) return s;
+    for (DevBuf &b : c->band_list)
+        if ((s = ensure(c, b, np * 4))) return s;
+    cudaStream_t st = c->stream;
+    c->last_launches = 0;
+    uint32_t *counters = (uint32_t *)c->counters.p;
+    uint32_t *ctr = (uint32_t *)c->band_ctr.p;      // [0] zero, [1..15] totals and queues, [32..33] cells
+    PA_CUDA(c, cudaEventRecord(c->ev0, st));
+    PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, st));
+    PA_CUDA(c, cudaMemsetAsync(c->band_ctr.p, 0, 256, st));
+    if ((s = enqueue_prep(c, P, C, s1, o1, s2, o2, out, np))) return s;
+    BandSpec *spec = (BandSpec *)c->band_spec.p;
+    if (h_bands) {
+        if ((s = ensure(c, c->band_in, np * 40))) return s;
+        PA_CUDA(c, cudaMemcpyAsync(c->band_in.p, h_bands, np * 40, cudaMemcpyHostToDevice, st));
+        band_from_ints_launch(st, (const int32_t *)c->band_in.p, np, spec);
+        c->last_launches++;
+    } else if (cfg->band_mode == 2) {
+        band_straight_launch(st, o1, o2, np, c->band_opt.straight_w0, c->band_opt.w_min, spec);
+        c->last_launches++;
+    } else if ((s = band_predict(c, P, s1, o1, s2, o2, np, spec))) {
+        return s;
+    }
+    uint32_t ranges[4], counts[3];
+    PA_CUDA(c, cudaMemcpyAsync(ranges, c->ranges.p, sizeof(ranges), cudaMemcpyDeviceToHost, st));
+    PA_CUDA(c, cudaMemcpyAsync(counts, c->counts.p, sizeof(counts), cudaMemcpyDeviceToHost, st));
+    PA_CUDA(c, cudaStreamSynchronize(st));
+
+    DpLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.seq1 = s1; L.off1 = o1; L.seq2 = s2; L.off2 = o2;
+    L.qtab = (const uint32_t *)c->qtab.p;
+    L.out = out;
+    L.boundary = (Cell *)c->boundary.p;
+    L.rerun_list = (uint32_t *)c->rerun.p;
+    L.rerun_count = counters + 4;
+    L.band_win = (const int2 *)c->band_win.p;
+    L.band = spec;
+    L.band_code = (uint8_t *)c->band_code.p;
+    L.dp_cells = (unsigned long long *)(ctr + 32);
+    // byte-compare class: the full DP
+    L.order = (const uint32_t *)c->order.p;
+    L.begin_ptr = (const uint32_t *)c->ranges.p + K_GEN;
+    L.count_ptr = (const uint32_t *)c->counts.p + K_GEN;
+    L.unit_counter = counters + 2;
+    L.G = c->G[K_GEN];
+    launch_class(c, K_GEN, M_GLOBAL, false, true, L, P);
+
+    uint32_t *lst[8];
+    for (int k = 0; k < 8; ++k) lst[k] = (uint32_t *)c->band_list[k].p;
+    uint32_t *cur16 = lst[0], *cur32 = lst[1], *nxt16 = lst[2], *nxt32 = lst[3], *full16 = lst[4],
+             *full32 = lst[5], *tmp = lst[6], *redo = lst[7];
+    uint32_t n16 = counts[K_S16], n32 = counts[K_S32], nf16 = 0, nf32 = 0;
+    if (n16) PA_CUDA(c, cudaMemcpyAsync(cur16, (const uint32_t *)c->order.p + ranges[K_S16], n16 * 4ull,
+                                        cudaMemcpyDeviceToDevice, st));
+    if (n32) PA_CUDA(c, cudaMemcpyAsync(cur32, (const uint32_t *)c->order.p + ranges[K_S32], n32 * 4ull,
+                                        cudaMemcpyDeviceToDevice, st));
+    uint64_t banded = 0, rounds = 0;
+    uint8_t *code = (uint8_t *)c->band_code.p;
+    uint32_t *bsum = (uint32_t *)c->band_bsum.p;
+    const float full_frac = c->band_opt.full_frac;
+    // one round of one lane width over `list`
+    auto band_step = [&](bool lanes16, const uint32_t *list, uint32_t count, int rows, int r, bool rerun,
+                         uint32_t *next, uint32_t &n_next, uint32_t *full, uint32_t &n_full, uint32_t *redo_out,
+                         uint32_t &n_redo) -> pa_status {
+        band_windows_launch(st, o1, o2, list, count, spec, rows, r, full_frac, (int2 *)c->band_win.p, code);
+        compact_launch(st, list, code, count, 2, bsum, full + n_full, ctr + 1);
+        compact_launch(st, list, code, count, 0, bsum, tmp, ctr + 2);
+        c->last_launches += 7;
+        uint32_t h[4];
+        PA_CUDA(c, cudaMemcpyAsync(h, ctr + 1, 8, cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaStreamSynchronize(st));
+        n_full += h[0];
+        const uint32_t nb = h[1];
+        if (nb == 0) return PA_OK;
+        PA_CUDA(c, cudaMemsetAsync(ctr + 3, 0, 4, st));
+        L.order = tmp;
+        L.begin_ptr = ctr + 0;
+        L.count_ptr = ctr + 2;
+        L.unit_counter = ctr + 3;
+        L.G = lanes16 ? c->G[K_S16] : c->G[K_S32];
+        L.band_rows = rows;
+        L.band_round = r;
+        L.rerun = rerun ? 1 : 0;
+        band_dp_launch(lanes16, band_dp_occupancy(lanes16) * c->sm_count, st, L, P);
+        compact_launch(st, tmp, code, nb, 1, bsum, next + n_next, ctr + 4);
+        compact_launch(st, tmp, code, nb, 3, bsum, redo_out ? redo_out : tmp, ctr + 5);
+        c->last_launches += 7;
+        PA_CUDA(c, cudaMemcpyAsync(h, ctr + 4, 8, cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaStreamSynchronize(st));
+        PA_CUDA(c, cudaGetLastError());
+        n_next += h[0];
+        n_redo = redo_out ? h[1] : 0;
+        banded += nb - h[0] - h[1];
+        return PA_OK;
+    };
+    for (int r = 0; r < c->band_opt.max_rounds && (n16 || n32); ++r) {
+        ++rounds;
+        uint32_t m16 = 0, m32 = 0, nredo = 0, none = 0;
+        if (n16 && (s = band_step(true, cur16, n16, rows16, r, false, nxt16, m16, full16, nf16, redo, nredo)))
+            return s;
+        if (nredo && (s = band_step(false, redo, nredo, rows32, r, true, nxt32, m32, full32, nf32, nullptr, none)))
+            return s;
+        if (n32 && (s = band_step(false, cur32, n32, rows32, r, false, nxt32, m32, full32, nf32, nullptr, none)))
+            return s;
+        std::swap(cur16, nxt16);
+        std::swap(cur32, nxt32);
+        n16 = m16;
+        n32 = m32;
+    }
+    // still open after the last round: full DP
+    if (n16) PA_CUDA(c, cudaMemcpyAsync(full16 + nf16, cur16, n16 * 4ull, cudaMemcpyDeviceToDevice, st));
+    if (n32) PA_CUDA(c, cudaMemcpyAsync(full32 + nf32, cur32, n32 * 4ull, cudaMemcpyDeviceToDevice, st));
+    nf16 += n16;
+    nf32 += n32;
+    const uint32_t hc[2] = {nf16, nf32};
+    PA_CUDA(c, cudaMemcpyAsync(ctr + 6, hc, 8, cudaMemcpyHostToDevice, st));
+    L.begin_ptr = ctr + 0;
+    L.rerun = 0;
+    if (nf16) {
+        L.order = full16; L.count_ptr = ctr + 6; L.unit_counter = ctr + 8; L.G = c->G[K_S16];
+        launch_class(c, K_S16, M_GLOBAL, true, false, L, P);
+        L.order = (const uint32_t *)c->rerun.p;     // s16 results that failed their check
+        L.begin_ptr = counters + 5;
+        L.count_ptr = counters + 4;
+        L.unit_counter = counters + 3;
+        L.rerun = 1;
+        L.G = c->G[K_S32];
+        launch_class(c, K_S32, M_GLOBAL, false, false, L, P);
+    }
+    if (nf32) {
+        L.order = full32; L.begin_ptr = ctr + 0; L.count_ptr = ctr + 7; L.unit_counter = ctr + 9;
+        L.rerun = 0; L.G = c->G[K_S32];
+        launch_class(c, K_S32, M_GLOBAL, false, false, L, P);
+    }
+    mark_full_launch(st, out, np);
+    c->last_launches++;
+    PA_CUDA(c, cudaEventRecord(c->ev1, st));
+    PA_CUDA(c, cudaStreamSynchronize(st));
+    PA_CUDA(c, cudaGetLastError());
+    PrepStats ps;
+    uint32_t rr = 0;
+    unsigned long long cells = 0;
+    PA_CUDA(c, cudaMemcpy(&ps, c->pstats.p, sizeof(ps), cudaMemcpyDeviceToHost));
+    PA_CUDA(c, cudaMemcpy(&rr, counters + 4, 4, cudaMemcpyDeviceToHost));
+    PA_CUDA(c, cudaMemcpy(&cells, ctr + 32, 8, cudaMemcpyDeviceToHost));
+    if (stats) {
+        stats->pairs = np;
+        stats->cells = ps.cells;
+        stats->pairs_s16 = ps.n_class[K_S16];
+        stats->pairs_s32 = ps.n_class[K_S32];
+        stats->pairs_general = ps.n_class[K_GEN];
+        stats->pairs_trivial = ps.n_class[K_NONE];
+        stats->pairs_rerun = rr;
+        stats->kernel_launches = c->last_launches;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        stats->device_ms = ms;
+        stats->dp_ms = ms;
+        stats->pairs_banded = banded;
+        stats->pairs_full_dp = nf16 + nf32 + ps.n_class[K_GEN];
+        stats->band_cells = cells;
+        stats->band_rounds = rounds;
+    }
+    if (ps.overflow) return fail(c, PA_ERR_OVERFLOW, "scores of some pairs could exceed int32");
+    return PA_OK;
+}
+
 pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uint64_t *o1, uint64_t b1,
                      const uint8_t *s2, const uint64_t *o2, uint64_t b2, uint64_t n_pairs, pa_result *out,
                      pa_stats *stats, bool sync_for_stats)
 {
-    if (cfg) {
-        const int mi = cfg->method == PA_METHOD_LOCAL ? 0 : 1;
-        if (!c->fixed_variant) {
-            c->variant[K_S16] = c->tuning.variant_s16[mi];
-            c->variant[K_S32] = c->variant[K_GEN] = c->tuning.variant_s32[mi];
-        }
-        if (!c->fixed_G) {
-            c->G[K_S16] = c->tuning.group_threads_s16[mi];
-            c->G[K_S32] = c->G[K_GEN] = c->tuning.group_threads_s32[mi];
-        }
-    }
+    if (cfg && cfg->band_mode) return run_band(c, cfg, s1, o1, b1, s2, o2, b2, n_pairs, out, nullptr, stats);
+    apply_tuning(c, cfg);
     DpParams P;
     ClassCfg C;
     pa_status s = check_config(c, cfg, P, C);
@@ -487,9 +753,15 @@ pa_status pa_destroy(pa_ctx *c)
     for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
     DevBuf *bufs[] = {&c->keys, &c->order, &c->hist, &c->starts, &c->cursor, &c->sums, &c->ranges,
                       &c->counts, &c->qtab, &c->boundary, &c->rerun, &c->counters, &c->pstats,
-                      &c->in_seq1, &c->in_off1, &c->in_seq2, &c->in_off2, &c->in_out};
+                      &c->in_seq1, &c->in_off1, &c->in_seq2, &c->in_off2, &c->in_out,
+                      &c->band_spec, &c->band_win, &c->band_code, &c->band_bsum, &c->band_ctr, &c->band_in,
+                      &c->mlp_feat, &c->mlp_x, &c->mlp_h1, &c->mlp_h2, &c->mlp_out};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
+    for (DevBuf &b : c->band_list)
+        if (b.p) cudaFree(b.p);
+    for (DevBuf &b : c->mlp_w)
+        if (b.p) cudaFree(b.p);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->ev2) cudaEventDestroy(c->ev2);
@@ -524,9 +796,82 @@ pa_status pa_align_batch_device(pa_ctx *ctx, const pa_config *config, const uint
     return PA_OK;
 }
 
+static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1, const uint64_t *off1,
+                            const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, pa_result *out,
+                            pa_stats *stats, const int32_t *bands);
+
 pa_status pa_align_batch(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1, const uint64_t *off1,
                          const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, pa_result *out,
                          pa_stats *stats)
+{
+    return align_host(ctx, config, seq1, off1, seq2, off2, n_pairs, out, stats, nullptr);
+}
+
+pa_status pa_align_batch_banded(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1, const uint64_t *off1,
+                                const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, const int32_t *bands,
+                                pa_result *out, pa_stats *stats)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    if (n_pairs && !bands) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "bands is null");
+    if (!config) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "config is null");
+    pa_config cfg = *config;
+    cfg.band_mode = 1;
+    return align_host(ctx, &cfg, seq1, off1, seq2, off2, n_pairs, out, stats, bands);
+}
+
+pa_status pa_set_band_options(pa_ctx *ctx, const pa_band_options *o)
+{
+    if (!ctx || !o) return PA_ERR_INVALID_ARGUMENT;
+    if (!(o->margin > 0.f) || o->w_min < 1 || o->straight_w0 < 1 || !(o->full_frac > 0.f) || o->max_rounds < 0 ||
+        o->max_rounds > 30)
+        return fail(ctx, PA_ERR_INVALID_ARGUMENT, "band options out of range");
+    ctx->band_opt = *o;
+    return PA_OK;
+}
+
+pa_status pa_get_band_options(const pa_ctx *ctx, pa_band_options *out)
+{
+    if (!ctx || !out) return PA_ERR_INVALID_ARGUMENT;
+    *out = ctx->band_opt;
+    return PA_OK;
+}
+
+pa_status pa_set_band_model(pa_ctx *ctx, const float *w1, const float *b1, const float *w2, const float *b2,
+                            const float *w3, const float *b3)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    if (!w1 || !b1 || !w2 || !b2 || !w3 || !b3) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null weight");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, PA_ERR_CUDA, "cudaSetDevice");
+    const float *src[6] = {w1, b1, w2, b2, w3, b3};
+    const int rows[6] = {144, 1, 256, 1, 256, 1}, cols[6] = {256, 256, 256, 256, 16, 16};
+    void *tmp = nullptr;
+    if (cudaMalloc(&tmp, 256 * 256 * 4) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, PA_ERR_OUT_OF_MEMORY, "band model upload");
+    }
+    pa_status s = PA_OK;
+    for (int k = 0; k < 6 && !s; ++k) {
+        const size_t n = (size_t)rows[k] * cols[k];
+        const bool weight = (k % 2) == 0;
+        if ((s = ensure(ctx, ctx->mlp_w[k], n * (weight ? 2 : 4)))) break;
+        bool ok;
+        if (weight)          // BF16 copy on the device, rounded as the training kernels round
+            ok = cudaMemcpy(tmp, src[k], n * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+                 pa_mlp_to_bf16((const float *)tmp, rows[k], cols[k], cols[k], ctx->mlp_w[k].p, nullptr) == PA_OK &&
+                 cudaDeviceSynchronize() == cudaSuccess;
+        else
+            ok = cudaMemcpy(ctx->mlp_w[k].p, src[k], n * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+        if (!ok) s = fail(ctx, PA_ERR_CUDA, "band model upload");
+    }
+    cudaFree(tmp);
+    if (s) return s;
+    ctx->has_model = true;
+    return PA_OK;
+}
+
+static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1, const uint64_t *off1,
+                            const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, pa_result *out,
+                            pa_stats *stats, const int32_t *bands)
 {
     if (!ctx) return PA_ERR_INVALID_ARGUMENT;
     if (n_pairs == 0) {
@@ -558,6 +903,15 @@ pa_status pa_align_batch(pa_ctx *ctx, const pa_config *config, const uint8_t *se
     if (b2) PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_seq2.p, seq2 + base2, b2, cudaMemcpyHostToDevice, st));
     PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off1.p, h1, (n_pairs + 1) * 8, cudaMemcpyHostToDevice, st));
     PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off2.p, h2, (n_pairs + 1) * 8, cudaMemcpyHostToDevice, st));
+    if (config && config->band_mode) {
+        s = run_band(ctx, config, (const uint8_t *)ctx->in_seq1.p, (const uint64_t *)ctx->in_off1.p, b1,
+                     (const uint8_t *)ctx->in_seq2.p, (const uint64_t *)ctx->in_off2.p, b2, n_pairs,
+                     (pa_result *)ctx->in_out.p, bands, stats);
+        if (s && s != PA_ERR_OVERFLOW) return s;
+        PA_CUDA(ctx, cudaMemcpyAsync(out, ctx->in_out.p, n_pairs * sizeof(pa_result), cudaMemcpyDeviceToHost, st));
+        PA_CUDA(ctx, cudaStreamSynchronize(st));
+        return s;
+    }
     s = run_device(ctx, config, (const uint8_t *)ctx->in_seq1.p, (const uint64_t *)ctx->in_off1.p, b1,
                    (const uint8_t *)ctx->in_seq2.p, (const uint64_t *)ctx->in_off2.p, b2, n_pairs,
                    (pa_result *)ctx->in_out.p, stats, false);
@@ -604,6 +958,104 @@ pa_status pa_align_one_to_many(pa_ctx *ctx, const pa_config *config, const uint8
     }
     qo[n_targets] = n_targets * query_len;
     return pa_align_batch(ctx, config, q.data(), qo.data(), targets, target_off, n_targets, out, stats);
+}
+
+pa_status pa_band_labels(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1, const uint64_t *off1,
+                         const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, int32_t *labels)
+{
+    if (!ctx || !config || (n_pairs && (!seq1 || !off1 || !seq2 || !off2 || !labels)))
+        return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null argument");
+    if (config->method != PA_METHOD_GLOBAL) return fail(ctx, PA_ERR_UNSUPPORTED, "band labels are for global alignment");
+    DpParams P;
+    ClassCfg C;
+    pa_status s = check_config(ctx, config, P, C);
+    if (s) return s;
+    if (n_pairs == 0) return PA_OK;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, PA_ERR_CUDA, "cudaSetDevice");
+    const uint64_t b1 = off1[n_pairs] - off1[0], b2 = off2[n_pairs] - off2[0];
+    // reversed copies of every pair, offsets rebased to 0
+    std::vector<uint8_t> r1(std::max<uint64_t>(b1, 1)), r2(std::max<uint64_t>(b2, 1));
+    std::vector<uint64_t> o1(n_pairs + 1), o2(n_pairs + 1);
+    for (uint64_t k = 0; k <= n_pairs; ++k) { o1[k] = off1[k] - off1[0]; o2[k] = off2[k] - off2[0]; }
+    for (uint64_t k = 0; k < n_pairs; ++k) {
+        const uint64_t m = o1[k + 1] - o1[k], n = o2[k + 1] - o2[k];
+        for (uint64_t x = 0; x < m; ++x) r1[o1[k] + x] = seq1[off1[0] + o1[k] + m - 1 - x];
+        for (uint64_t x = 0; x < n; ++x) r2[o2[k] + x] = seq2[off2[0] + o2[k] + n - 1 - x];
+    }
+    std::memset(labels, 0, sizeof(int32_t) * 8 * n_pairs);
+    std::vector<void *> bufs;
+    auto dalloc = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+        bufs.push_back(p);
+        return p;
+    };
+    auto cleanup = [&]() { for (void *p : bufs) cudaFree(p); };
+    uint8_t *d1 = (uint8_t *)dalloc(b1), *d2 = (uint8_t *)dalloc(b2), *dr1 = (uint8_t *)dalloc(b1),
+            *dr2 = (uint8_t *)dalloc(b2);
+    uint64_t *do1 = (uint64_t *)dalloc(8 * (n_pairs + 1)), *do2 = (uint64_t *)dalloc(8 * (n_pairs + 1));
+    uint64_t *ddoff = (uint64_t *)dalloc(8 * n_pairs);
+    int32_t *dlab = (int32_t *)dalloc(sizeof(int32_t) * 8 * n_pairs);
+    pa_result *dout = (pa_result *)dalloc(sizeof(pa_result) * n_pairs);
+    Cell *dbound = (Cell *)dalloc(sizeof(Cell) * (b1 + n_pairs));
+    uint32_t *dorder = (uint32_t *)dalloc(4 * n_pairs), *dctr = (uint32_t *)dalloc(64);
+    const uint64_t kDumpBudget = 64ull << 20;                    // int32 entries per chunk (256 MB)
+    int32_t *ddump = (int32_t *)dalloc(4 * kDumpBudget);
+    if (!d1 || !d2 || !dr1 || !dr2 || !do1 || !do2 || !ddoff || !dlab || !dout || !dbound || !dorder || !dctr || !ddump) {
+        cleanup();
+        return fail(ctx, PA_ERR_OUT_OF_MEMORY, "band labels: cudaMalloc failed");
+    }
+    cudaStream_t st = ctx->stream;
+    bool ok = cudaMemcpyAsync(d1, seq1 + off1[0], b1, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(d2, seq2 + off2[0], b2, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(dr1, r1.data(), b1, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(dr2, r2.data(), b2, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(do1, o1.data(), 8 * (n_pairs + 1), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(do2, o2.data(), 8 * (n_pairs + 1), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemsetAsync(dlab, 0, sizeof(int32_t) * 8 * n_pairs, st) == cudaSuccess;
+    const int grid = band_labels_occupancy() * ctx->sm_count;
+    std::vector<uint64_t> doff(n_pairs, 0);
+    std::vector<uint32_t> order;
+    uint64_t k = 0;
+    while (ok && k < n_pairs) {
+        order.clear();
+        uint64_t used = 0;
+        for (; k < n_pairs; ++k) {
+            const uint64_t m = o1[k + 1] - o1[k], n = o2[k + 1] - o2[k];
+            if (m < 9 || n == 0) continue;                        // checkpoints need 9 columns
+            const uint64_t need = 8 * (n + 1);
+            if (need > kDumpBudget) { ok = false; break; }
+            if (used + need > kDumpBudget) break;
+            doff[k] = used;
+            used += need;
+            order.push_back((uint32_t)k);
+        }
+        if (!ok || order.empty()) break;
+        const uint32_t ctr[2] = {0u, (uint32_t)order.size()};   // begin, count
+        ok = cudaMemcpyAsync(ddoff, doff.data(), 8 * n_pairs, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+             cudaMemcpyAsync(dorder, order.data(), 4 * order.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+             cudaMemcpyAsync(dctr + 8, ctr, sizeof(ctr), cudaMemcpyHostToDevice, st) == cudaSuccess;
+        for (int rev = 0; ok && rev < 2; ++rev) {
+            DpLaunch L;
+            std::memset(&L, 0, sizeof(L));
+            L.seq1 = rev ? dr1 : d1; L.off1 = do1; L.seq2 = rev ? dr2 : d2; L.off2 = do2;
+            L.order = dorder; L.begin_ptr = dctr + 8; L.count_ptr = dctr + 9; L.unit_counter = dctr;
+            L.out = dout; L.boundary = dbound; L.G = 8;
+            L.dump = ddump; L.dump_off = ddoff; L.labels = dlab;
+            ok = cudaMemsetAsync(dctr, 0, 4, st) == cudaSuccess;
+            if (ok) band_labels_launch(rev == 1, grid, st, L, P);
+            ok = ok && cudaGetLastError() == cudaSuccess;
+        }
+        ok = ok && cudaStreamSynchronize(st) == cudaSuccess;      // the host staging arrays are reused
+    }
+    ok = ok && cudaMemcpyAsync(labels, dlab, sizeof(int32_t) * 8 * n_pairs, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+         cudaStreamSynchronize(st) == cudaSuccess;
+    cleanup();
+    if (!ok) {
+        cudaGetLastError();
+        return fail(ctx, PA_ERR_CUDA, "band labels: a CUDA call failed or a pair exceeds the dump budget");
+    }
+    return PA_OK;
 }
 
 pa_status pa_get_tuning(const pa_ctx *ctx, pa_tuning *out)

@@ -31,6 +31,15 @@ struct __align__(8) Cell {
     uint32_t h, e;
 };
 
+// Band of one pair (band mode): the centre line runs through (0, 0), the 8
+// checkpoints (i_c, i_c + diag[c]) with i_c = (c + 1) * m / 9, and (m, n); the
+// half-width tapers linearly from w_start at column 0 to w_min at column m.
+struct BandSpec {
+    int32_t diag[8];
+    int32_t w_start, w_min;
+    int32_t pad[2];
+};
+
 // Per-launch description of a DP class.
 struct DpLaunch {
     const uint8_t *seq1;          // streamed sequences (raw bytes)
@@ -49,6 +58,19 @@ struct DpLaunch {
     unsigned long long *dp_cells; // statistics: cells computed (incl. padding), may be null
     int32_t G;                    // threads per group (1..32, power of two)
     int32_t rerun;                // this launch consumes a rerun list
+    // label modes (training data of the band predictor): H at 8 checkpoint columns
+    int32_t *dump;                // forward pass: dump[dump_off[p] + c * (n + 1) + j] = H(i_c, j)
+    const uint64_t *dump_off;     // per pair offset into dump
+    int32_t *labels;              // reverse pass: 8 optimal-path diagonals (j - i_c) per pair
+    // band mode: per-pass column windows {first, last} (1-based) of every pair, at
+    // slot (off2[id] - off2[0]) / band_rows + id; the outcome of list position k goes
+    // to band_code[k]: 0 certified, 1 not certified (widen), 3 redo in s32 lanes
+    const int2 *band_win;
+    BandSpec *band;
+    uint8_t *band_code;
+    int32_t *band_ub;             // optional: the largest exit bound per pair
+    int32_t band_rows;            // rows per pass of the window table (G * R)
+    int32_t band_round;
 };
 
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)

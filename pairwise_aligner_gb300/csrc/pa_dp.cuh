@@ -45,7 +45,15 @@
 
 namespace pa {
 
-enum Mode : int { M_LOCAL = 0, M_GLOBAL = 1, M_GLOBAL_FREE = 2 };
+enum Mode : int { M_LOCAL = 0, M_GLOBAL = 1, M_GLOBAL_FREE = 2, M_LABEL_FWD = 3, M_LABEL_REV = 4, M_BAND = 5 };
+
+// "Minus infinity" of band mode: cells outside the band.  s16x2 lanes use the
+// clamp floor (its exactness check covers it), s32 lanes a value far below any
+// score that gaps can still be subtracted from without wrapping.
+constexpr int32_t kNeg32 = -(1 << 30);
+
+// Checkpoint columns of the band labels: i_c = c * m / 9, c = 1..8.
+__device__ __forceinline__ int32_t checkpoint_col(int c, int32_t m) { return (int32_t)(((int64_t)(c + 1) * m) / 9); }
 
 // ---- lane arithmetic policies ------------------------------------------------
 struct L16 {
@@ -139,7 +147,31 @@ struct GroupWork {
     const uint32_t *qt[2];
     Cell *buf;
     int32_t cs[2], ci[2], cj[2];   // candidate (score, end1, end2) per lane
+    int32_t lb_v[8], lb_j[8];      // label mode: best forward + reverse score per checkpoint and its row
+    // band mode: columns ibase+1 .. iend of the current pass; thread 0's first diagonal
+    int32_t ibase, iend;
+    uint32_t diag0;
+    int32_t ub[2];                 // largest bound on a path that leaves the band, per lane
+    unsigned long long cells;      // band cells computed (statistics)
 };
+
+// Upper bound on the score of a path that enters cell (i, j) from inside the band
+// and then runs to (m, n): `gapv` is the score of entering in a gap state, `diagv`
+// by a diagonal step.  From (i, j) at most min(m - i, n - j) diagonal steps gain
+// smax each, and the diagonal changes by d = |(n - j) - (m - i)|, which costs at
+// least d gap extensions (the gap may continue the entering one) or, after a
+// diagonal step, one gap open and d extensions.
+__device__ __forceinline__ int32_t exit_bound(const DpParams &P, int32_t gapv, int32_t diagv, int32_t i, int32_t j,
+                                              int32_t m, int32_t n)
+{
+    const int64_t ri = m - i, rj = n - j;
+    const int64_t d = ri > rj ? ri - rj : rj - ri;
+    const int64_t gain = (int64_t)P.smax * (ri < rj ? ri : rj);
+    const int64_t g = gapv + gain + (int64_t)P.gap_ext * d;
+    const int64_t h = diagv + gain + (d ? (int64_t)P.gap_open + (int64_t)P.gap_ext * d : 0);
+    const int64_t b = g > h ? g : h;
+    return b > INT32_MAX ? INT32_MAX : (b < INT32_MIN ? INT32_MIN : (int32_t)b);
+}
 
 template <class V>
 __device__ __forceinline__ uint32_t stored(const GroupWork &w, int32_t true_value)
@@ -162,6 +194,13 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
     const uint32_t CLAMP = w.CLAMP;
     const uint32_t CLAMPG = V::LANES == 2 ? V::subc(CLAMP, GOEA) : (uint32_t)max((int)CLAMP, INT32_MIN + 65536) - GOEA;
 
+    constexpr bool BAND = MODE == M_BAND;
+    const int32_t ibase = BAND ? w.ibase : 0;      // the pass sweeps columns ibase+1 .. iend
+    const int32_t iend = BAND ? w.iend : w.ms;
+    const int32_t msw = iend - ibase;
+    const bool left_out = BAND && ibase > 0;        // column ibase lies outside the band
+    const uint32_t NEGV = V::LANES == 2 ? CLAMP : (uint32_t)kNeg32;
+
     uint32_t H[RA], Fr[RA], Sel[RA];
 #pragma unroll
     for (int k = 0; k < RA; ++k) {
@@ -173,11 +212,12 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             else c[l] = (j < w.n[l]) ? (int)dna_code(L.seq2[w.toff[l] + j]) : -1;
         }
         Sel[k] = GEN ? (uint32_t)c[0] : V::selector(c[0], c[1]);
-        H[k] = stored<V>(w, border(P, P.first_row_free, (int64_t)j + 1));
+        H[k] = left_out ? NEGV : stored<V>(w, border(P, P.first_row_free, (int64_t)j + 1));
         Fr[k] = V::subc(H[k], GOEA);
     }
-    uint32_t prevH = stored<V>(w, border(P, P.first_row_free, j0));
+    uint32_t prevH = left_out ? (t == 0 ? w.diag0 : NEGV) : stored<V>(w, border(P, P.first_row_free, j0));
     uint32_t topH = prevH;                              // thread 0, pass 0: H(i-1, 0)
+    uint32_t top_last = NEGV;                           // band: thread 0's top input at column iend
     const uint32_t step1 = P.first_column_free ? 0u : V::cabs(P.gap_open + P.gap_ext);
     const uint32_t stepn = P.first_column_free ? 0u : EXTA;
     uint32_t outH = 0, outE = 0, best = w.K;
@@ -192,7 +232,6 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
         own_t[l] = r / RA;
         own_k[l] = r - own_t[l] * RA;
     }
-    const int32_t ms = w.ms;
     const bool last_pass = p + 1 == w.passes;
     // next column's score tables, loaded one step ahead
     uint32_t nta = 0, ntb = 0;
@@ -206,7 +245,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
         }
     };
     Cell nbuf = Cell{0u, 0u};                        // thread 0, pass > 0: next boundary cell
-    if (t == 0 && p > 0) nbuf = w.buf[1];
+    if (t == 0 && p > 0) nbuf = w.buf[ibase + 1];
     constexpr bool TUNED = (VAR & 4) != 0;
     const bool first_thread = t == 0;
     const bool top_border = first_thread && p == 0;
@@ -220,10 +259,10 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             const uint32_t nt = V::max2(V::subc(topH, i == 1 ? step1 : stepn), CLAMP);
             topH = top_border ? nt : topH;
             const Cell c = nbuf;
-            if (top_buffer && i < ms) nbuf = w.buf[i + 1];
+            if (top_buffer && i < iend) nbuf = w.buf[i + 1];
             upH = top_border ? nt : (top_buffer ? c.h : upH);
             upE = top_border ? V::subc(nt, GOEA) : (top_buffer ? c.e : upE);
-            if (!GEN && i + 8 <= ms) {
+            if (!GEN && i + 8 <= iend) {
                 asm volatile("prefetch.global.L1 [%0];" ::"l"(w.qt[0] + min(i + 7, w.m[0])));
                 if (NL == 2) asm volatile("prefetch.global.L1 [%0];" ::"l"(w.qt[1] + min(i + 7, w.m[1])));
             }
@@ -235,11 +274,12 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             } else {
                 upH = nbuf.h;
                 upE = nbuf.e;
-                if (i < ms) nbuf = w.buf[i + 1];
+                if (i < iend) nbuf = w.buf[i + 1];
             }
         }
+        if (BAND && i == iend) top_last = upH;
         const uint32_t ta = nta, tb = ntb;
-        if (i < ms) load_tables(i + 1, nta, ntb);
+        if (i < iend) load_tables(i + 1, nta, ntb);
         uint32_t diag = prevH, Ed = upE;
 #pragma unroll
         for (int k = 0; k < RA; ++k) {
@@ -279,6 +319,31 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
         outE = Ed;
         if (t == G - 1 && !last_pass) w.buf[i] = Cell{outH, outE};
 
+        if (MODE == M_LABEL_FWD || MODE == M_LABEL_REV) {
+            // forward: keep the checkpoint columns; reverse (sequences reversed): column i is
+            // the forward column m - i, row j the forward row n - j
+            const int32_t m0 = w.m[0], n0 = w.n[0];
+            for (int c = 0; c < 8; ++c) {
+                const int32_t col = MODE == M_LABEL_FWD ? checkpoint_col(c, m0) : m0 - checkpoint_col(c, m0);
+                if (col != i) continue;
+                int32_t *dc = L.dump + L.dump_off[w.id[0]] + (uint64_t)c * (n0 + 1);
+                if (MODE == M_LABEL_FWD) {
+                    if (t == 0 && p == 0) dc[0] = border(P, P.first_column_free, i);
+#pragma unroll
+                    for (int k = 0; k < RA; ++k)
+                        if (j0 + k + 1 <= n0) dc[j0 + k + 1] = V::get(H[k], 0) - w.Kt;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < RA; ++k) {
+                        const int32_t jf = n0 - (j0 + k + 1);            // forward row
+                        if (jf >= 0) {
+                            const int32_t v = dc[jf] + V::get(H[k], 0) - w.Kt;
+                            if (v > w.lb_v[c] || (v == w.lb_v[c] && jf < w.lb_j[c])) { w.lb_v[c] = v; w.lb_j[c] = jf; }
+                        }
+                    }
+                }
+            }
+        }
         if (MODE == M_LOCAL) {
             uint32_t cm = H[0];
 #pragma unroll
@@ -331,18 +396,36 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
         }
     };
     // fill: thread t starts at step t (steps 0..G-1); steady: every thread active; drain
-    if (t == 0) load_tables(1, nta, ntb);
-    const int32_t fill_end = min(G, ms + G - 1);
+    if (t == 0) load_tables(ibase + 1, nta, ntb);
+    const int32_t fill_end = min(G, msw + G - 1);
     int s = 0;
     for (; s < fill_end; ++s) {
-        const int32_t i = s - t + 1;
-        if (i == 1 && t > 0) load_tables(1, nta, ntb);
-        step(i, i >= 1 && i <= ms);
+        const int32_t li = s - t + 1;
+        if (li == 1 && t > 0) load_tables(ibase + 1, nta, ntb);
+        step(ibase + li, li >= 1 && li <= msw);
     }
-    for (; s < ms; ++s) step(s - t + 1, true);
-    for (; s < ms + G - 1; ++s) {
-        const int32_t i = s - t + 1;
-        step(i, i >= 1 && i <= ms);
+    for (; s < msw; ++s) step(ibase + s - t + 1, true);
+    for (; s < msw + G - 1; ++s) {
+        const int32_t li = s - t + 1;
+        step(ibase + li, li >= 1 && li <= msw);
+    }
+    if (BAND) {
+        // exits through the right edge: cells (iend + 1, j) of this pass's rows, entered
+        // by a horizontal gap from (iend, j) or diagonally from (iend, j - 1)
+        const uint32_t above = __shfl_up_sync(gmask, H[RA - 1], 1, G);
+        const uint32_t hup0 = t == 0 ? top_last : above;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
+            if ((l == 1 && !w.has_b) || iend >= w.m[l]) continue;
+#pragma unroll
+            for (int k = 0; k < RA; ++k) {
+                const int32_t j = j0 + k + 1;
+                if (j > w.n[l]) continue;
+                const int32_t gv = V::get(Fr[k], l) - w.Kt;
+                const int32_t dv = V::get(k == 0 ? hup0 : H[k - 1], l) - w.Kt + P.smax;
+                w.ub[l] = max(w.ub[l], exit_bound(P, gv, dv, iend + 1, j, w.m[l], w.n[l]));
+            }
+        }
     }
     if (MODE == M_LOCAL) {
 #pragma unroll
@@ -405,6 +488,9 @@ __global__ void __launch_bounds__(kBlock, MINB) dp_kernel(DpLaunch L, DpParams P
             w.ci[l] = 0;
             w.cj[l] = 0;
         }
+        for (int c = 0; c < 8; ++c) { w.lb_v[c] = INT32_MIN; w.lb_j[c] = 0; }
+        w.ub[0] = w.ub[1] = INT32_MIN;
+        w.cells = 0;
         w.ms = NL == 2 ? max(w.m[0], w.m[1]) : w.m[0];
         w.nh = NL == 2 ? max(w.n[0], w.n[1]) : w.n[0];
         w.rows_full = G * R;
@@ -432,9 +518,38 @@ __global__ void __launch_bounds__(kBlock, MINB) dp_kernel(DpLaunch L, DpParams P
             w.CLAMP = (uint32_t)w.clampt;
         }
 
+        // band mode: the column window of each pass is the union of the lanes' windows,
+        // kept monotone and overlapping the previous pass by at least one column
+        int2 bcur = make_int2(1, w.ms), bprev = make_int2(1, w.ms);
+        auto band_window = [&](int p, int2 prev) -> int2 {
+            int32_t a = INT32_MAX, b = 0;
+#pragma unroll
+            for (int l = 0; l < NL; ++l) {
+                if (l == 1 && !w.has_b) continue;
+                if ((int64_t)p * w.rows_full >= w.n[l]) continue;
+                const uint64_t slot = (L.off2[w.id[l]] - L.off2[0]) / (uint64_t)L.band_rows + w.id[l];
+                const int2 x = L.band_win[slot + p];
+                a = min(a, x.x);
+                b = max(b, x.y);
+            }
+            if (a == INT32_MAX) { a = 1; b = w.ms; }
+            if (p > 0) { a = max(min(a, prev.y), prev.x); b = max(b, prev.y); }
+            a = p == 0 ? 1 : max(a, 1);
+            b = min(max(b, a), w.ms);
+            return make_int2(a, b);
+        };
+        const uint32_t NEGV = MODE == M_BAND ? (NL == 2 ? w.CLAMP : (uint32_t)kNeg32) : 0u;
+        if (MODE == M_BAND) bcur = band_window(0, bprev);
+
         for (int p = 0; p < w.passes; ++p) {
             const int32_t rem = w.nh - p * w.rows_full;
             const int32_t rpt = rem >= w.rows_full ? R : ((rem + G * kChunk - 1) / (G * kChunk)) * kChunk;
+            if (MODE == M_BAND) {
+                w.ibase = bcur.x - 1;
+                w.iend = bcur.y;
+                const int32_t c0 = bcur.x - 1;
+                w.diag0 = (p > 0 && c0 >= bprev.x && c0 <= bprev.y) ? w.buf[c0].h : NEGV;
+            }
             switch (rpt / kChunk) {
             case 1: run_pass<V, R, 4, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
             case 2: run_pass<V, R, 8, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
@@ -442,11 +557,59 @@ __global__ void __launch_bounds__(kBlock, MINB) dp_kernel(DpLaunch L, DpParams P
             default: run_pass<V, R, R, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
             }
             __syncwarp(gmask);
+            if (MODE == M_BAND) {
+                const bool more = p + 1 < w.passes;
+                const int2 bnext = more ? band_window(p + 1, bcur) : bcur;
+                const int32_t jlo = p * w.rows_full + 1, jhi = p * w.rows_full + G * rpt;
+                const int32_t goe = P.gap_open + P.gap_ext;
+#pragma unroll
+                for (int l = 0; l < NL; ++l) {
+                    if (l == 1 && !w.has_b) continue;
+                    const int32_t ml = w.m[l], nl = w.n[l];
+                    if (jlo > nl) continue;
+                    if (t == 0) w.cells += (unsigned long long)(bcur.y - bcur.x + 1) * (min(jhi, nl) - jlo + 1);
+                    if (p == 0)       // along the top border past the window, then down into row 1
+                        for (int32_t i = bcur.y + 1 + t; i <= ml; i += G)
+                            w.ub[l] = max(w.ub[l], exit_bound(P, border(P, 0, i) + goe, border(P, 0, i - 1) + P.smax,
+                                                              i, 1, ml, nl));
+                    if (bcur.x > 1)   // down the left border, then into column 1 of this pass
+                        for (int32_t j = jlo + t; j <= min(jhi, nl); j += G)
+                            w.ub[l] = max(w.ub[l], exit_bound(P, border(P, 0, j) + goe, border(P, 0, j - 1) + P.smax,
+                                                              1, j, ml, nl));
+                    if (more && jhi < nl) {   // through the bottom edge left of the next window
+                        const int32_t last = min(min(bcur.y, bnext.x - 1), ml);
+                        for (int32_t i = bcur.x + t; i <= last; i += G) {
+                            const Cell c = w.buf[i];
+                            w.ub[l] = max(w.ub[l], exit_bound(P, V::get(c.e, l) - w.Kt, kNeg32, i, jhi + 1, ml, nl));
+                            if (i + 1 < bnext.x)
+                                w.ub[l] = max(w.ub[l], exit_bound(P, kNeg32, V::get(c.h, l) - w.Kt + P.smax, i + 1,
+                                                                  jhi + 1, ml, nl));
+                        }
+                    }
+                }
+                if (more)             // columns the next pass reads beyond this window: outside
+                    for (int32_t i = bcur.y + 1 + t; i <= bnext.y; i += G) w.buf[i] = Cell{NEGV, NEGV};
+                __syncwarp(gmask);
+                bprev = bcur;
+                bcur = bnext;
+            }
         }
 
+        if (MODE == M_LABEL_REV) {
+            for (int c = 0; c < 8; ++c) {
+                for (int off = G >> 1; off >= 1; off >>= 1) {
+                    const int32_t ov = __shfl_xor_sync(gmask, w.lb_v[c], off, G);
+                    const int32_t oj = __shfl_xor_sync(gmask, w.lb_j[c], off, G);
+                    if (ov > w.lb_v[c] || (ov == w.lb_v[c] && oj < w.lb_j[c])) { w.lb_v[c] = ov; w.lb_j[c] = oj; }
+                }
+                if (t == 0) L.labels[(uint64_t)w.id[0] * 8 + c] = w.lb_j[c] - checkpoint_col(c, w.m[0]);
+            }
+        }
         // group reduction of the candidates
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
+            if (MODE == M_BAND)
+                for (int off = G >> 1; off >= 1; off >>= 1) w.ub[l] = max(w.ub[l], __shfl_xor_sync(gmask, w.ub[l], off, G));
             for (int off = G >> 1; off >= 1; off >>= 1) {
                 const int32_t os = __shfl_xor_sync(gmask, w.cs[l], off, G);
                 const int32_t oi = __shfl_xor_sync(gmask, w.ci[l], off, G);
@@ -476,6 +639,22 @@ __global__ void __launch_bounds__(kBlock, MINB) dp_kernel(DpLaunch L, DpParams P
                 r.flags = L.rerun ? PA_RESULT_RERUN : 0;
                 r.band_rounds = 0;
                 if (MODE == M_LOCAL && w.cs[l] <= 0) { r.end1 = 0; r.end2 = 0; }
+                if (MODE == M_BAND) {
+                    uint8_t code;
+                    if (NL == 2 && (int64_t)w.cs[l] <= (int64_t)w.floor_true + (int64_t)P.smax * min(w.m[l], w.n[l])) {
+                        code = 3;                           // a clamp may have reached it: redo in s32
+                    } else if (w.cs[l] != INT32_MIN && w.ub[l] <= w.cs[l]) {   // no path leaving the band scores more
+                        r.flags |= PA_RESULT_BANDED;
+                        r.band_rounds = (uint16_t)L.band_round;
+                        L.out[w.id[l]] = r;
+                        code = 0;
+                    } else {
+                        code = 1;
+                    }
+                    L.band_code[first + l] = code;
+                    if (L.band_ub) L.band_ub[w.id[l]] = w.ub[l];
+                    continue;
+                }
                 if (NL == 2 && MODE != M_LOCAL &&
                     (int64_t)w.cs[l] <= (int64_t)w.floor_true + (int64_t)P.smax * min(w.m[l], w.n[l])) {
                     // a clamp may have reached this result: recompute the pair in s32
@@ -486,6 +665,7 @@ __global__ void __launch_bounds__(kBlock, MINB) dp_kernel(DpLaunch L, DpParams P
                 L.out[w.id[l]] = r;
             }
         }
+        if (MODE == M_BAND && t == 0 && L.dp_cells && w.cells) atomicAdd(L.dp_cells, w.cells);
         __syncwarp(gmask);
     }
 }

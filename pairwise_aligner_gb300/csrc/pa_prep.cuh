@@ -78,11 +78,20 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint32_t match4 = (uint8_t)P.match * 0x01010101u;
     const uint32_t mis4 = (uint8_t)P.mismatch * 0x01010101u;
+    // statistics are summed per lane 0 and per block, then added once per block
+    unsigned long long my_cells = 0, my_class[4] = {0, 0, 0, 0}, my_overflow = 0;
     for (uint64_t p = warp; p < n_pairs; p += nwarps) {
         const uint64_t q0 = off1[p], t0 = off2[p];
         const int64_t m = (int64_t)(off1[p + 1] - q0), n = (int64_t)(off2[p + 1] - t0);
         bool dna = true;
-        for (int64_t j = lane; j < n; j += 32) dna &= dna_valid(seq2[t0 + j]);
+        for (int64_t j = 4 * lane; j < n; j += 128) {     // four independent loads per lane
+            const uint8_t *q = seq2 + t0 + j;
+            const int64_t left = n - j;
+            dna &= dna_valid(q[0]);
+            if (left > 1) dna &= dna_valid(q[1]);
+            if (left > 2) dna &= dna_valid(q[2]);
+            if (left > 3) dna &= dna_valid(q[3]);
+        }
         dna = __all_sync(0xffffffffu, dna);
         uint32_t klass;
         if (m == 0 || n == 0) klass = K_NONE;
@@ -91,15 +100,19 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
         else klass = K_S32;
         if (klass == K_S16 || klass == K_S32) {
             uint32_t *qt = qtab + q0 + p;
-            for (int64_t i = lane; i <= m; i += 32)
-                qt[i] = (i < m) ? score_table(seq1[q0 + i], match4, mis4) : 0x80808080u;
+            for (int64_t i = 4 * lane; i <= m; i += 128) {
+                const uint8_t *a = seq1 + q0 + i;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (i + u <= m) qt[i + u] = (i + u < m) ? score_table(a[u], match4, mis4) : 0x80808080u;
+            }
         }
         if (lane == 0) {
             const int64_t a = P.match < 0 ? -(int64_t)P.match : P.match;
             const int64_t b = P.mismatch < 0 ? -(int64_t)P.mismatch : P.mismatch;
             const int64_t o = -(int64_t)P.gap_open, e = -(int64_t)P.gap_ext;
             const int64_t bound = (a + b) * min(m, n) + (o + e) * (m + n + 2) + 2 * o;
-            if (bound >= (1ll << 30)) atomicAdd(&st->overflow, 1ull);
+            if (bound >= (1ll << 30)) ++my_overflow;
             uint32_t key;
             if (klass == K_NONE) {
                 pa_result r;
@@ -114,12 +127,28 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
                 const uint64_t shape = (uint64_t)(passes - 1) * (R / 4) + (uint64_t)(nch - 1);
                 key = (klass << kClassShift) | (quant_shape(shape > 0xffffffffull ? 0xffffffffu : (uint32_t)shape) << 10) |
                       quant_len((uint32_t)m);
-                atomicAdd(&st->cells, (unsigned long long)(m * n));
+                my_cells += (unsigned long long)(m * n);
             }
             keys[p] = key;
             atomicAdd(&hist[key], 1u);
-            atomicAdd(&st->n_class[klass], 1ull);
+            ++my_class[klass];
         }
+    }
+    __shared__ unsigned long long sh[6];
+    if (threadIdx.x < 6) sh[threadIdx.x] = 0;
+    __syncthreads();
+    if (lane == 0) {
+        if (my_cells) atomicAdd(&sh[0], my_cells);
+        for (int k = 0; k < 4; ++k)
+            if (my_class[k]) atomicAdd(&sh[1 + k], my_class[k]);
+        if (my_overflow) atomicAdd(&sh[5], my_overflow);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (sh[0]) atomicAdd(&st->cells, sh[0]);
+        for (int k = 0; k < 4; ++k)
+            if (sh[1 + k]) atomicAdd(&st->n_class[k], sh[1 + k]);
+        if (sh[5]) atomicAdd(&st->overflow, sh[5]);
     }
 }
 

@@ -37,6 +37,26 @@ def test_python_binding_covers_the_header(built_lib):
     assert set(declared_functions()) <= set(_lib.SIGNATURES)
 
 
+def declared_arity():
+    """name -> number of parameters of every prototype in include/*.h."""
+    out = {}
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for name, args in re.findall(r"\b(pa_\w+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+            args = args.strip()
+            out[name] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_python_binding_argument_counts_match_the_header(built_lib):
+    from pairwise_aligner_gb300 import _lib
+    arity = declared_arity()
+    assert len(arity) >= 20
+    wrong = {n: (k, len(_lib.SIGNATURES[n][0])) for n, k in arity.items() if len(_lib.SIGNATURES[n][0]) != k}
+    assert not wrong, wrong
+
+
 def test_status_strings_and_version(built_lib):
     from pairwise_aligner_gb300 import _lib
     lib = _lib.load()
@@ -50,7 +70,8 @@ def test_struct_layouts_match_header(built_lib):
     from pairwise_aligner_gb300 import _lib
     assert ctypes.sizeof(_lib.PaResult) == 16
     assert ctypes.sizeof(_lib.PaConfig) == 32
-    assert ctypes.sizeof(_lib.PaStats) == 8 * 10
+    assert ctypes.sizeof(_lib.PaStats) == 8 * 14
+    assert ctypes.sizeof(_lib.PaBandOptions) == 32
 
 
 def test_create_without_gpu_reports_no_device(built_lib):

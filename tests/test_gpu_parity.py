@@ -6,6 +6,8 @@ batches of the benchmark configurations compared with the oracle.
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 import pytest
 
@@ -242,3 +244,21 @@ def test_autotune_keeps_results_exact(pa, oracle, tmp_path):
     fresh = pa.Context(0)
     fresh.load_tuning(path)
     assert fresh.tuning()["variant_s16"] == t["variant_s16"]
+
+
+def test_config5_stratified_sample(pa, oracle):
+    """Mixed global stream: short, long and very long (20-50 kb + structural indels) pairs in one batch."""
+    from pairwise_aligner_gb300 import workloads as W
+    d = W.config5(seed=5, n_pairs=400, strata=(0.90, 0.085, 0.015))
+    al = _aligner_for(pa, d)
+    res = al.compute_arrays(d["seq1"], d["off1"], d["seq2"], d["off2"])
+    _check(oracle, d, res, nthreads=os.cpu_count())
+    st = al.last_stats
+    assert st["pairs_s16"] + st["pairs_s32"] == 400
+
+
+def test_config4_sample(pa, oracle):
+    from pairwise_aligner_gb300 import workloads as W
+    d = W.config4(seed=4, n_pairs=2048)
+    res = _aligner_for(pa, d).compute_arrays(d["seq1"], d["off1"], d["seq2"], d["off2"])
+    _check(oracle, d, res)
