@@ -214,6 +214,11 @@ pa_status pa_mlp_adam(float *w, void *w16, const float *grad, float *m1, float *
                       void *stream);
 pa_status pa_mlp_to_bf16(const float *src, int rows, int cols, int ld_dst, void *dst, void *stream);
 
+/* Pairs with at least `cells` = m * n cells are computed by whole thread blocks
+ * (the warps of a block pipeline the pair's row passes) instead of one group of
+ * lanes; default 2^22.  1 sends every pair there, UINT64_MAX none. */
+pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells);
+
 /* Band mode (no counterpart in the reference, which has no banded mode).
  * A pair's band: the centre line through (0, 0), the checkpoints
  * (i_c, i_c + diag[c]) with i_c = (c + 1) * m / 9, c = 0..7, and (m, n),

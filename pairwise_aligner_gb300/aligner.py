@@ -61,6 +61,10 @@ class Context:
         except Exception:
             pass
 
+    def set_cta_threshold(self, cells: int):
+        """Pairs with at least `cells` m*n cells run on whole thread blocks (1: all pairs)."""
+        _lib.check(self.lib.pa_set_cta_threshold(self.ptr, int(cells)), self.ptr)
+
     # -- band mode ----------------------------------------------------------------
     def band_options(self) -> dict:
         o = _lib.PaBandOptions()

@@ -18,6 +18,8 @@
 //             a set fraction of the matrix, the pair goes to the full DP.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "pa_dp.cuh"
 
 namespace pa {
@@ -253,13 +255,16 @@ __global__ void k_mark_full(pa_result *__restrict__ out, uint64_t n_pairs)
 namespace {
 constexpr int kBandVar = 12;     // branch-free top input + two-op vertical-gap chain
 
-template <class V>
+template <class V, bool CTA>
 int band_occ()
 {
     static int per_sm = -1;
     if (per_sm < 0) {
         int v = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel<V, 16, M_BAND, false, kBandVar, 2>, kBlock, 0);
+        if (CTA)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel_cta<V, 16, M_BAND, false, kBandVar>, kBlock, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel<V, 16, M_BAND, false, kBandVar, 2>, kBlock, 0);
         per_sm = v < 1 ? 1 : v;
     }
     return per_sm;
@@ -267,12 +272,25 @@ int band_occ()
 inline unsigned blocks(uint64_t n, unsigned per) { return (unsigned)((n + per - 1) / per); }
 }  // namespace
 
-int band_dp_occupancy(bool lanes16) { return lanes16 ? band_occ<L16>() : band_occ<L32>(); }
-
-void band_dp_launch(bool lanes16, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
+int band_dp_occupancy(bool lanes16, bool cta)
 {
-    if (lanes16) dp_kernel<L16, 16, M_BAND, false, kBandVar, 2><<<grid, kBlock, 0, st>>>(L, P);
-    else dp_kernel<L32, 16, M_BAND, false, kBandVar, 2><<<grid, kBlock, 0, st>>>(L, P);
+    if (cta) return lanes16 ? band_occ<L16, true>() : band_occ<L32, true>();
+    return lanes16 ? band_occ<L16, false>() : band_occ<L32, false>();
+}
+
+int band_cta_occupancy() { return std::max(band_dp_occupancy(true, true), band_dp_occupancy(false, true)); }
+
+// CTA launches use the ring rows of L (grid blocks of 8 rows each).
+void band_dp_launch(bool lanes16, bool cta, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
+{
+    if (cta) {
+        if (lanes16) dp_kernel_cta<L16, 16, M_BAND, false, kBandVar><<<grid, kBlock, 0, st>>>(L, P);
+        else dp_kernel_cta<L32, 16, M_BAND, false, kBandVar><<<grid, kBlock, 0, st>>>(L, P);
+    } else if (lanes16) {
+        dp_kernel<L16, 16, M_BAND, false, kBandVar, 2><<<grid, kBlock, 0, st>>>(L, P);
+    } else {
+        dp_kernel<L32, 16, M_BAND, false, kBandVar, 2><<<grid, kBlock, 0, st>>>(L, P);
+    }
 }
 
 void band_windows_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, const uint32_t *list,

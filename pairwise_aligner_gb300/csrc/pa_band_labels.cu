@@ -22,6 +22,21 @@ void band_labels_launch(bool reverse, int grid, cudaStream_t st, const DpLaunch 
     else dp_kernel<L32, 16, M_LABEL_FWD, true, 0><<<grid, kBlock, 0, st>>>(L, P);
 }
 
+// Long pairs: whole blocks per pair (CTA mode), L.ring holding grid * 8 rows.
+void band_labels_cta_launch(bool reverse, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
+{
+    if (reverse) dp_kernel_cta<L32, 16, M_LABEL_REV, true, 0><<<grid, kBlock, 0, st>>>(L, P);
+    else dp_kernel_cta<L32, 16, M_LABEL_FWD, true, 0><<<grid, kBlock, 0, st>>>(L, P);
+}
+
+int band_labels_cta_occupancy()
+{
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, dp_kernel_cta<L32, 16, M_LABEL_FWD, true, 0>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, dp_kernel_cta<L32, 16, M_LABEL_REV, true, 0>, kBlock, 0);
+    return std::max(1, std::min(a, b));
+}
+
 int band_labels_occupancy()
 {
     int a = 0, b = 0;

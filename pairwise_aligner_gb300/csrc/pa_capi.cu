@@ -31,6 +31,7 @@ namespace {
 
 
 constexpr int kR = 16;             // rows per thread per lane
+constexpr int64_t kDefaultRingM = 65536;   // device entry points: CTA mode up to this sequence1 length
 constexpr int kDefaultG = 8;       // threads per group
 
 struct DevBuf {
@@ -57,6 +58,11 @@ struct pa_ctx {
     std::string err;
     // device work buffers (grow only)
     DevBuf keys, order, hist, starts, cursor, sums, ranges, counts, qtab, boundary, rerun, counters, pstats;
+    DevBuf ring, rerun_long;      // CTA mode: boundary rows per block; s16 long pairs to redo in s32
+    int32_t ring_m = 0;           // longest sequence1 the ring rows hold (0: no CTA mode yet)
+    int ring_grid = 0;            // blocks of every CTA-mode launch
+    int64_t long_cells = 1ll << 22;   // pairs with at least this many cells use CTA mode
+    int64_t want_ring_m = 0;          // the next call's longest CTA-mode sequence1 (host: exact)
     DevBuf in_seq1, in_off1, in_seq2, in_off2, in_out;   // staging for the host-buffer entry points
     int G[3] = {kDefaultG, kDefaultG, kDefaultG};
     int variant[3] = {0, 0, 0};
@@ -68,7 +74,7 @@ struct pa_ctx {
     // band mode
     pa_band_options band_opt{1.25f, 16, 64, 0.5f, 6, {0, 0, 0}};
     DevBuf band_spec, band_win, band_code, band_bsum, band_ctr, band_in;
-    DevBuf band_list[8];
+    DevBuf band_list[16];
     DevBuf mlp_w[6], mlp_feat, mlp_x, mlp_h1, mlp_h2, mlp_out;
     bool has_model = false;
 };
@@ -138,11 +144,14 @@ pa_status check_config(pa_ctx *c, const pa_config *cfg, DpParams &P, ClassCfg &C
     C.s16_params = (int64_t)cfg->gap_open + cfg->gap_extension >= -1000 && cfg->gap_extension >= -1000;
     C.force32 = cfg->width_hint == 32;
     C.local = local;
-    for (int k = 0; k < 3; ++k) {
-        C.gcnt[k] = c->G[k];
+    for (int k = 0; k < kClasses; ++k) {
+        const bool cta = k >= (int)kLongOffset;
+        C.gcnt[k] = cta ? 32 : c->G[k < 3 ? k : 0];
         C.rpt[k] = kR;
-        C.rows[k] = c->G[k] * kR;
+        C.rows[k] = C.gcnt[k] * kR;
     }
+    C.long_cells = c->long_cells;
+    C.long_max_m = c->ring.p ? c->ring_m : 0;
     return PA_OK;
 }
 
@@ -170,9 +179,12 @@ int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
 }
 
 void band_labels_launch(bool reverse, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
+void band_labels_cta_launch(bool reverse, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
 int band_labels_occupancy();
-int band_dp_occupancy(bool lanes16);
-void band_dp_launch(bool lanes16, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
+int band_labels_cta_occupancy();
+int band_dp_occupancy(bool lanes16, bool cta);
+int band_cta_occupancy();
+void band_dp_launch(bool lanes16, bool cta, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
 void band_windows_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, const uint32_t *list,
                          uint32_t count, const BandSpec *spec, int32_t rows, int shift, float full_frac, int2 *win,
                          uint8_t *code);
@@ -234,7 +246,7 @@ pa_status enqueue_prep(pa_ctx *c, const DpParams &P, const ClassCfg &C, const ui
                                               (PrepStats *)c->pstats.p);
     k_scan_blocks<<<kBuckets / 1024, 1024, 0, st>>>((uint32_t *)c->hist.p, (uint32_t *)c->starts.p,
                                                     (uint32_t *)c->sums.p);
-    k_scan_sums<<<1, 256, 0, st>>>((uint32_t *)c->sums.p, kBuckets / 1024);
+    k_scan_sums<<<1, kBuckets / 1024, 0, st>>>((uint32_t *)c->sums.p, kBuckets / 1024);
     k_scan_add<<<kBuckets / 1024, 1024, 0, st>>>((uint32_t *)c->starts.p, (uint32_t *)c->cursor.p,
                                                  (uint32_t *)c->sums.p, (uint32_t *)c->ranges.p);
     const int sc_blocks = (int)std::max<uint64_t>(1, (n_pairs + kBlock - 1) / kBlock);
@@ -284,6 +296,30 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
     // byte-compare class
     L.begin_ptr = ranges + K_GEN; L.count_ptr = counts + K_GEN; L.unit_counter = counters + 2; L.G = c->G[K_GEN];
     launch_class(c, K_GEN, mode, false, true, L, P);
+    // long pairs: whole blocks per pair; their s16 results that fail the check are redone in s32
+    if (c->ring.p) {
+        DpLaunch LL = L;
+        LL.ring = (Cell *)c->ring.p;
+        LL.ring_stride = (uint64_t)c->ring_m + 2;
+        LL.error = counters + 8;
+        LL.rerun_list = (uint32_t *)c->rerun_long.p;
+        LL.rerun_count = counters + 6;
+        LL.G = 32;
+        const Klass lc[3] = {K_S16L, K_S32L, K_GENL};
+        for (int k = 0; k < 3; ++k) {
+            LL.begin_ptr = ranges + lc[k]; LL.count_ptr = counts + lc[k]; LL.unit_counter = counters + 9 + k;
+            dp_cta_launch(k == 0, k == 2, mode, c->ring_grid, st, LL, P);
+        }
+        if (mode != M_LOCAL) {
+            LL.order = (const uint32_t *)c->rerun_long.p;
+            LL.begin_ptr = counters + 5;
+            LL.count_ptr = counters + 6;
+            LL.unit_counter = counters + 12;
+            LL.rerun = 1;
+            dp_cta_launch(false, false, mode, c->ring_grid, st, LL, P);
+        }
+        c->last_launches += mode != M_LOCAL ? 4 : 3;
+    }
     // s16 global results that failed the exactness check, recomputed in s32
     if (mode != M_LOCAL) {
         L.order = (const uint32_t *)c->rerun.p;
@@ -300,6 +336,29 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
     return PA_OK;
 }
 
+// Ring rows of CTA mode for sequence1 lengths up to `max_m` (grow only).
+pa_status ensure_ring(pa_ctx *c, int64_t max_m)
+{
+    if (max_m <= 0) return PA_OK;
+    if (max_m > (1 << 20)) max_m = 1 << 20;
+    if (c->ring.p && c->ring_m >= max_m) return PA_OK;
+    int per_sm = 1;
+    for (int mode = 0; mode < 3; ++mode) {
+        per_sm = std::max(per_sm, dp_cta_occupancy(true, false, mode));
+        per_sm = std::max(per_sm, dp_cta_occupancy(false, false, mode));
+        per_sm = std::max(per_sm, dp_cta_occupancy(false, true, mode));
+    }
+    per_sm = std::max(per_sm, band_cta_occupancy());
+    per_sm = std::max(per_sm, band_labels_cta_occupancy());
+    const int grid = per_sm * c->sm_count;
+    const int32_t m = (int32_t)std::max<int64_t>(max_m, c->ring_m);
+    pa_status s = ensure(c, c->ring, (size_t)grid * 8 * ((size_t)m + 2) * sizeof(Cell));
+    if (s) return s;
+    c->ring_m = m;
+    c->ring_grid = grid;
+    return PA_OK;
+}
+
 pa_status prepare_buffers(pa_ctx *c, uint64_t n_pairs, uint64_t b1)
 {
     pa_status s;
@@ -307,6 +366,7 @@ pa_status prepare_buffers(pa_ctx *c, uint64_t n_pairs, uint64_t b1)
     if ((s = ensure(c, c->keys, np * 4))) return s;
     if ((s = ensure(c, c->order, np * 4))) return s;
     if ((s = ensure(c, c->rerun, np * 4))) return s;
+    if ((s = ensure(c, c->rerun_long, np * 4))) return s;
     if ((s = ensure(c, c->hist, sizeof(uint32_t) * kBuckets))) return s;
     if ((s = ensure(c, c->starts, sizeof(uint32_t) * kBuckets))) return s;
     if ((s = ensure(c, c->cursor, sizeof(uint32_t) * kBuckets))) return s;
@@ -366,19 +426,22 @@ pa_status band_predict(pa_ctx *c, const DpParams &P, const uint8_t *s1, const ui
     return PA_OK;
 }
 
+pa_status read_stats(pa_ctx *c, pa_stats *stats);
+
 // Band mode (host-synchronous between rounds): classify and sort as the plain
-// path, build every pair's band, then per round and lane width: windows ->
-// (too wide: full DP list) -> banded DP -> certified results, pairs to widen,
+// path, build every pair's band, then per round and work class: windows ->
+// (too wide: full-DP list) -> banded DP -> certified results, pairs to widen,
 // and s16 results to redo in s32; finally the full DP for what is left.
 pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uint64_t *o1, uint64_t b1,
                    const uint8_t *s2, const uint64_t *o2, uint64_t b2, uint64_t n_pairs, pa_result *out,
                    const int32_t *h_bands, pa_stats *stats)
 {
     apply_tuning(c, cfg);
+    pa_status s = n_pairs ? ensure_ring(c, c->want_ring_m) : PA_OK;
+    if (s) return s;
     DpParams P;
     ClassCfg C;
-    pa_status s = check_config(c, cfg, P, C);
-    if (s) return s;
+    if ((s = check_config(c, cfg, P, C))) return s;
     if (P.local || P.first_column_free || P.first_row_free || P.last_column_free || P.last_row_free)
         return fail(c, PA_ERR_UNSUPPORTED, "band mode needs global alignment with penalised end gaps");
     if (!h_bands && cfg->band_mode == 1 && !c->has_model)
@@ -389,9 +452,17 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     if (n_pairs >= (1ull << 31)) return fail(c, PA_ERR_TOO_LARGE, "n_pairs must be < 2^31");
     if ((s = prepare_buffers(c, n_pairs, b1))) return s;
     const uint64_t np = n_pairs;
-    const int rows16 = c->G[K_S16] * kR, rows32 = c->G[K_S32] * kR;
+    // the band work classes: {lanes16, cta} -> s16 groups, s32 groups, s16 blocks, s32 blocks
+    struct BandClass {
+        bool lanes16, cta;
+        Klass klass;
+        int rows;
+    };
+    const BandClass bc[4] = {{true, false, K_S16, c->G[K_S16] * kR}, {false, false, K_S32, c->G[K_S32] * kR},
+                             {true, true, K_S16L, 32 * kR}, {false, true, K_S32L, 32 * kR}};
+    const int min_rows = std::min(std::min(bc[0].rows, bc[1].rows), 32 * kR);
     if ((s = ensure(c, c->band_spec, np * sizeof(BandSpec)))) return s;
-    if ((s = ensure(c, c->band_win, (b2 / std::min(rows16, rows32) + np + 1) * sizeof(int2)))) return s;
+    if ((s = ensure(c, c->band_win, (b2 / min_rows + np + 1) * sizeof(int2)))) return s;
     if ((s = ensure(c, c->band_code, np))) return s;
     if ((s = ensure(c, c->band_bsum, (np / 1024 + 2) * 4))) return s;
     if ((s = ensure(c, c->band_ctr, 256))) return s;
@@ -400,7 +471,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     cudaStream_t st = c->stream;
     c->last_launches = 0;
     uint32_t *counters = (uint32_t *)c->counters.p;
-    uint32_t *ctr = (uint32_t *)c->band_ctr.p;      // [0] zero, [1..15] totals and queues, [32..33] cells
+    uint32_t *ctr = (uint32_t *)c->band_ctr.p;      // [0] zero, [1..31] totals and queues, [32..33] cells
     PA_CUDA(c, cudaEventRecord(c->ev0, st));
     PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, st));
     PA_CUDA(c, cudaMemsetAsync(c->band_ctr.p, 0, 256, st));
@@ -417,9 +488,9 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     } else if ((s = band_predict(c, P, s1, o1, s2, o2, np, spec))) {
         return s;
     }
-    uint32_t ranges[4], counts[3];
+    uint32_t ranges[8], counts[8];
     PA_CUDA(c, cudaMemcpyAsync(ranges, c->ranges.p, sizeof(ranges), cudaMemcpyDeviceToHost, st));
-    PA_CUDA(c, cudaMemcpyAsync(counts, c->counts.p, sizeof(counts), cudaMemcpyDeviceToHost, st));
+    PA_CUDA(c, cudaMemcpyAsync(counts, c->counts.p, 4 * kClasses, cudaMemcpyDeviceToHost, st));
     PA_CUDA(c, cudaStreamSynchronize(st));
 
     DpLaunch L;
@@ -428,45 +499,82 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     L.qtab = (const uint32_t *)c->qtab.p;
     L.out = out;
     L.boundary = (Cell *)c->boundary.p;
-    L.rerun_list = (uint32_t *)c->rerun.p;
-    L.rerun_count = counters + 4;
     L.band_win = (const int2 *)c->band_win.p;
     L.band = spec;
     L.band_code = (uint8_t *)c->band_code.p;
     L.dp_cells = (unsigned long long *)(ctr + 32);
-    // byte-compare class: the full DP
-    L.order = (const uint32_t *)c->order.p;
-    L.begin_ptr = (const uint32_t *)c->ranges.p + K_GEN;
-    L.count_ptr = (const uint32_t *)c->counts.p + K_GEN;
-    L.unit_counter = counters + 2;
-    L.G = c->G[K_GEN];
-    launch_class(c, K_GEN, M_GLOBAL, false, true, L, P);
+    L.ring = (Cell *)c->ring.p;
+    L.ring_stride = (uint64_t)c->ring_m + 2;
+    L.error = counters + 8;
+    // the full DP of a list: group kernels (with the s16 -> s32 redo list) or whole blocks
+    auto full_dp = [&](int k, const uint32_t *list, uint32_t *count_word, uint32_t *queue) {
+        DpLaunch F = L;
+        F.order = list;
+        F.begin_ptr = ctr + 0;
+        F.count_ptr = count_word;
+        F.unit_counter = queue;
+        F.rerun = 0;
+        F.rerun_list = (uint32_t *)(bc[k].cta ? c->rerun_long.p : c->rerun.p);
+        F.rerun_count = counters + (bc[k].cta ? 6 : 4);
+        if (bc[k].cta) {
+            F.G = 32;
+            dp_cta_launch(bc[k].lanes16, false, M_GLOBAL, c->ring_grid, st, F, P);
+            c->last_launches++;
+        } else {
+            F.G = c->G[bc[k].klass];
+            launch_class(c, bc[k].klass, M_GLOBAL, bc[k].lanes16, false, F, P);
+        }
+    };
+    // byte-compare classes: the full DP
+    {
+        DpLaunch F = L;
+        F.order = (const uint32_t *)c->order.p;
+        F.rerun_list = (uint32_t *)c->rerun.p;
+        F.rerun_count = counters + 4;
+        F.begin_ptr = (const uint32_t *)c->ranges.p + K_GEN;
+        F.count_ptr = (const uint32_t *)c->counts.p + K_GEN;
+        F.unit_counter = counters + 2;
+        F.G = c->G[K_GEN];
+        launch_class(c, K_GEN, M_GLOBAL, false, true, F, P);
+        if (counts[K_GENL]) {
+            F.begin_ptr = (const uint32_t *)c->ranges.p + K_GENL;
+            F.count_ptr = (const uint32_t *)c->counts.p + K_GENL;
+            F.unit_counter = counters + 11;
+            F.G = 32;
+            dp_cta_launch(false, true, M_GLOBAL, c->ring_grid, st, F, P);
+            c->last_launches++;
+        }
+    }
 
-    uint32_t *lst[8];
-    for (int k = 0; k < 8; ++k) lst[k] = (uint32_t *)c->band_list[k].p;
-    uint32_t *cur16 = lst[0], *cur32 = lst[1], *nxt16 = lst[2], *nxt32 = lst[3], *full16 = lst[4],
-             *full32 = lst[5], *tmp = lst[6], *redo = lst[7];
-    uint32_t n16 = counts[K_S16], n32 = counts[K_S32], nf16 = 0, nf32 = 0;
-    if (n16) PA_CUDA(c, cudaMemcpyAsync(cur16, (const uint32_t *)c->order.p + ranges[K_S16], n16 * 4ull,
-                                        cudaMemcpyDeviceToDevice, st));
-    if (n32) PA_CUDA(c, cudaMemcpyAsync(cur32, (const uint32_t *)c->order.p + ranges[K_S32], n32 * 4ull,
-                                        cudaMemcpyDeviceToDevice, st));
+    uint32_t *lst[16];
+    for (int k = 0; k < 16; ++k) lst[k] = (uint32_t *)c->band_list[k].p;
+    uint32_t *cur[4] = {lst[0], lst[1], lst[2], lst[3]}, *nxt[4] = {lst[4], lst[5], lst[6], lst[7]},
+             *full[4] = {lst[8], lst[9], lst[10], lst[11]};
+    uint32_t *tmp = lst[12], *redo = lst[13];
+    uint32_t ncur[4], nfull[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; ++k) {
+        ncur[k] = counts[bc[k].klass];
+        if (ncur[k])
+            PA_CUDA(c, cudaMemcpyAsync(cur[k], (const uint32_t *)c->order.p + ranges[bc[k].klass], ncur[k] * 4ull,
+                                       cudaMemcpyDeviceToDevice, st));
+    }
     uint64_t banded = 0, rounds = 0;
     uint8_t *code = (uint8_t *)c->band_code.p;
     uint32_t *bsum = (uint32_t *)c->band_bsum.p;
     const float full_frac = c->band_opt.full_frac;
-    // one round of one lane width over `list`
-    auto band_step = [&](bool lanes16, const uint32_t *list, uint32_t count, int rows, int r, bool rerun,
-                         uint32_t *next, uint32_t &n_next, uint32_t *full, uint32_t &n_full, uint32_t *redo_out,
-                         uint32_t &n_redo) -> pa_status {
-        band_windows_launch(st, o1, o2, list, count, spec, rows, r, full_frac, (int2 *)c->band_win.p, code);
-        compact_launch(st, list, code, count, 2, bsum, full + n_full, ctr + 1);
+    // one round of work class k over `list`: pairs to widen go to next, s16 results to redo
+    // in s32 to redo_out (or nowhere)
+    auto band_step = [&](int k, const uint32_t *list, uint32_t count, int r, bool rerun, uint32_t *next,
+                         uint32_t &n_next, uint32_t *redo_out, uint32_t &n_redo) -> pa_status {
+        const BandClass &B = bc[k];
+        band_windows_launch(st, o1, o2, list, count, spec, B.rows, r, full_frac, (int2 *)c->band_win.p, code);
+        compact_launch(st, list, code, count, 2, bsum, full[k] + nfull[k], ctr + 1);
         compact_launch(st, list, code, count, 0, bsum, tmp, ctr + 2);
         c->last_launches += 7;
-        uint32_t h[4];
+        uint32_t h[2];
         PA_CUDA(c, cudaMemcpyAsync(h, ctr + 1, 8, cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaStreamSynchronize(st));
-        n_full += h[0];
+        nfull[k] += h[0];
         const uint32_t nb = h[1];
         if (nb == 0) return PA_OK;
         PA_CUDA(c, cudaMemsetAsync(ctr + 3, 0, 4, st));
@@ -474,11 +582,12 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         L.begin_ptr = ctr + 0;
         L.count_ptr = ctr + 2;
         L.unit_counter = ctr + 3;
-        L.G = lanes16 ? c->G[K_S16] : c->G[K_S32];
-        L.band_rows = rows;
+        L.G = B.cta ? 32 : c->G[B.klass];
+        L.band_rows = B.rows;
         L.band_round = r;
         L.rerun = rerun ? 1 : 0;
-        band_dp_launch(lanes16, band_dp_occupancy(lanes16) * c->sm_count, st, L, P);
+        band_dp_launch(B.lanes16, B.cta, B.cta ? c->ring_grid : band_dp_occupancy(B.lanes16, false) * c->sm_count,
+                       st, L, P);
         compact_launch(st, tmp, code, nb, 1, bsum, next + n_next, ctr + 4);
         compact_launch(st, tmp, code, nb, 3, bsum, redo_out ? redo_out : tmp, ctr + 5);
         c->last_launches += 7;
@@ -490,74 +599,100 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         banded += nb - h[0] - h[1];
         return PA_OK;
     };
-    for (int r = 0; r < c->band_opt.max_rounds && (n16 || n32); ++r) {
+    auto open_pairs = [&]() { return ncur[0] + ncur[1] + ncur[2] + ncur[3]; };
+    for (int r = 0; r < c->band_opt.max_rounds && open_pairs(); ++r) {
         ++rounds;
-        uint32_t m16 = 0, m32 = 0, nredo = 0, none = 0;
-        if (n16 && (s = band_step(true, cur16, n16, rows16, r, false, nxt16, m16, full16, nf16, redo, nredo)))
-            return s;
-        if (nredo && (s = band_step(false, redo, nredo, rows32, r, true, nxt32, m32, full32, nf32, nullptr, none)))
-            return s;
-        if (n32 && (s = band_step(false, cur32, n32, rows32, r, false, nxt32, m32, full32, nf32, nullptr, none)))
-            return s;
-        std::swap(cur16, nxt16);
-        std::swap(cur32, nxt32);
-        n16 = m16;
-        n32 = m32;
+        uint32_t nn[4] = {0, 0, 0, 0};
+        for (int k16 : {0, 2}) {                      // s16 classes, then their s32 redo, then s32
+            uint32_t nredo = 0, none = 0;
+            if (ncur[k16] && (s = band_step(k16, cur[k16], ncur[k16], r, false, nxt[k16], nn[k16], redo, nredo)))
+                return s;
+            if (nredo && (s = band_step(k16 + 1, redo, nredo, r, true, nxt[k16 + 1], nn[k16 + 1], nullptr, none)))
+                return s;
+            if (ncur[k16 + 1] &&
+                (s = band_step(k16 + 1, cur[k16 + 1], ncur[k16 + 1], r, false, nxt[k16 + 1], nn[k16 + 1], nullptr, none)))
+                return s;
+        }
+        for (int k = 0; k < 4; ++k) {
+            std::swap(cur[k], nxt[k]);
+            ncur[k] = nn[k];
+        }
     }
     // still open after the last round: full DP
-    if (n16) PA_CUDA(c, cudaMemcpyAsync(full16 + nf16, cur16, n16 * 4ull, cudaMemcpyDeviceToDevice, st));
-    if (n32) PA_CUDA(c, cudaMemcpyAsync(full32 + nf32, cur32, n32 * 4ull, cudaMemcpyDeviceToDevice, st));
-    nf16 += n16;
-    nf32 += n32;
-    const uint32_t hc[2] = {nf16, nf32};
-    PA_CUDA(c, cudaMemcpyAsync(ctr + 6, hc, 8, cudaMemcpyHostToDevice, st));
-    L.begin_ptr = ctr + 0;
-    L.rerun = 0;
-    if (nf16) {
-        L.order = full16; L.count_ptr = ctr + 6; L.unit_counter = ctr + 8; L.G = c->G[K_S16];
-        launch_class(c, K_S16, M_GLOBAL, true, false, L, P);
-        L.order = (const uint32_t *)c->rerun.p;     // s16 results that failed their check
-        L.begin_ptr = counters + 5;
-        L.count_ptr = counters + 4;
-        L.unit_counter = counters + 3;
-        L.rerun = 1;
-        L.G = c->G[K_S32];
-        launch_class(c, K_S32, M_GLOBAL, false, false, L, P);
+    uint32_t hc[8];
+    for (int k = 0; k < 4; ++k) {
+        if (ncur[k])
+            PA_CUDA(c, cudaMemcpyAsync(full[k] + nfull[k], cur[k], ncur[k] * 4ull, cudaMemcpyDeviceToDevice, st));
+        nfull[k] += ncur[k];
+        hc[k] = nfull[k];
     }
-    if (nf32) {
-        L.order = full32; L.begin_ptr = ctr + 0; L.count_ptr = ctr + 7; L.unit_counter = ctr + 9;
-        L.rerun = 0; L.G = c->G[K_S32];
-        launch_class(c, K_S32, M_GLOBAL, false, false, L, P);
+    PA_CUDA(c, cudaMemcpyAsync(ctr + 6, hc, 16, cudaMemcpyHostToDevice, st));
+    for (int k = 0; k < 4; ++k)
+        if (nfull[k]) full_dp(k, full[k], ctr + 6 + k, ctr + 10 + k);
+    if (nfull[0]) {                                   // s16 group results that failed their check
+        DpLaunch F = L;
+        F.order = (const uint32_t *)c->rerun.p;
+        F.begin_ptr = counters + 5;
+        F.count_ptr = counters + 4;
+        F.unit_counter = counters + 3;
+        F.rerun = 1;
+        F.G = c->G[K_S32];
+        launch_class(c, K_S32, M_GLOBAL, false, false, F, P);
+    }
+    if (nfull[2]) {                                   // the same for s16 long pairs
+        DpLaunch F = L;
+        F.order = (const uint32_t *)c->rerun_long.p;
+        F.begin_ptr = counters + 5;
+        F.count_ptr = counters + 6;
+        F.unit_counter = counters + 12;
+        F.rerun = 1;
+        F.G = 32;
+        dp_cta_launch(false, false, M_GLOBAL, c->ring_grid, st, F, P);
+        c->last_launches++;
     }
     mark_full_launch(st, out, np);
     c->last_launches++;
     PA_CUDA(c, cudaEventRecord(c->ev1, st));
     PA_CUDA(c, cudaStreamSynchronize(st));
     PA_CUDA(c, cudaGetLastError());
-    PrepStats ps;
-    uint32_t rr = 0;
     unsigned long long cells = 0;
-    PA_CUDA(c, cudaMemcpy(&ps, c->pstats.p, sizeof(ps), cudaMemcpyDeviceToHost));
-    PA_CUDA(c, cudaMemcpy(&rr, counters + 4, 4, cudaMemcpyDeviceToHost));
     PA_CUDA(c, cudaMemcpy(&cells, ctr + 32, 8, cudaMemcpyDeviceToHost));
+    pa_stats local;
+    pa_stats *st_out = stats ? stats : &local;
+    std::memset(st_out, 0, sizeof(*st_out));
+    s = read_stats(c, st_out);
+    st_out->pairs = np;
+    st_out->kernel_launches = c->last_launches;
+    st_out->dp_ms = st_out->device_ms;
+    st_out->pairs_banded = banded;
+    st_out->pairs_full_dp = nfull[0] + nfull[1] + nfull[2] + nfull[3] + counts[K_GEN] + counts[K_GENL];
+    st_out->band_cells = cells;
+    st_out->band_rounds = rounds;
+    return s;
+}
+
+// Counters of the finished call (after a sync): class sizes, reruns, error bits.
+pa_status read_stats(pa_ctx *c, pa_stats *stats)
+{
+    PrepStats ps;
+    uint32_t ctr[16];
+    PA_CUDA(c, cudaMemcpy(&ps, c->pstats.p, sizeof(ps), cudaMemcpyDeviceToHost));
+    PA_CUDA(c, cudaMemcpy(ctr, c->counters.p, sizeof(ctr), cudaMemcpyDeviceToHost));
     if (stats) {
-        stats->pairs = np;
-        stats->cells = ps.cells;
-        stats->pairs_s16 = ps.n_class[K_S16];
-        stats->pairs_s32 = ps.n_class[K_S32];
-        stats->pairs_general = ps.n_class[K_GEN];
-        stats->pairs_trivial = ps.n_class[K_NONE];
-        stats->pairs_rerun = rr;
-        stats->kernel_launches = c->last_launches;
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
         stats->device_ms = ms;
-        stats->dp_ms = ms;
-        stats->pairs_banded = banded;
-        stats->pairs_full_dp = nf16 + nf32 + ps.n_class[K_GEN];
-        stats->band_cells = cells;
-        stats->band_rounds = rounds;
+        if (cudaEventElapsedTime(&ms, c->ev_dp0, c->ev_dp1) == cudaSuccess) stats->dp_ms = ms;
+        cudaGetLastError();
+        const uint64_t rr = (uint64_t)ctr[4] + ctr[6];
+        stats->cells = ps.cells;
+        stats->pairs_s16 = ps.n_class[K_S16] + ps.n_class[K_S16L] - rr;
+        stats->pairs_s32 = ps.n_class[K_S32] + ps.n_class[K_S32L] + rr;
+        stats->pairs_general = ps.n_class[K_GEN] + ps.n_class[K_GENL];
+        stats->pairs_trivial = ps.n_class[K_NONE];
+        stats->pairs_rerun = rr;
     }
+    if (ctr[8]) return fail(c, PA_ERR_TIMEOUT, "a CTA-mode progress wait ran out");
     if (ps.overflow) return fail(c, PA_ERR_OVERFLOW, "scores of some pairs could exceed int32");
     return PA_OK;
 }
@@ -568,9 +703,11 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
 {
     if (cfg && cfg->band_mode) return run_band(c, cfg, s1, o1, b1, s2, o2, b2, n_pairs, out, nullptr, stats);
     apply_tuning(c, cfg);
+    pa_status s = n_pairs ? ensure_ring(c, c->want_ring_m) : PA_OK;
+    if (s) return s;
     DpParams P;
     ClassCfg C;
-    pa_status s = check_config(c, cfg, P, C);
+    s = check_config(c, cfg, P, C);
     if (s) return s;
     if (n_pairs == 0) {
         if (stats) std::memset(stats, 0, sizeof(*stats));
@@ -602,7 +739,7 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
             if (ce != cudaSuccess) return fail(c, PA_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ce));
             it = c->graphs.emplace(key, ex).first;
         } else {
-            c->last_launches = 6 + 3 + (P.local ? 0 : 1);
+            c->last_launches = 6 + 3 + (P.local ? 0 : 1) + (c->ring.p ? (P.local ? 3 : 4) : 0);
         }
         PA_CUDA(c, cudaGraphLaunch(it->second, c->stream));
     } else {
@@ -615,22 +752,7 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
         stats->kernel_launches = c->last_launches;
         if (sync_for_stats) {
             PA_CUDA(c, cudaEventSynchronize(c->ev1));
-            PrepStats ps;
-            uint32_t ctr[8];
-            PA_CUDA(c, cudaMemcpy(&ps, c->pstats.p, sizeof(ps), cudaMemcpyDeviceToHost));
-            PA_CUDA(c, cudaMemcpy(ctr, c->counters.p, sizeof(ctr), cudaMemcpyDeviceToHost));
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-            stats->device_ms = ms;
-            if (cudaEventElapsedTime(&ms, c->ev_dp0, c->ev_dp1) == cudaSuccess) stats->dp_ms = ms;
-            cudaGetLastError();
-            stats->cells = ps.cells;
-            stats->pairs_s16 = ps.n_class[K_S16] - ctr[4];
-            stats->pairs_s32 = ps.n_class[K_S32] + ctr[4];
-            stats->pairs_general = ps.n_class[K_GEN];
-            stats->pairs_trivial = ps.n_class[K_NONE];
-            stats->pairs_rerun = ctr[4];
-            if (ps.overflow) return fail(c, PA_ERR_OVERFLOW, "scores of some pairs could exceed int32");
+            if ((s = read_stats(c, stats))) return s;
         }
     }
     PA_CUDA(c, cudaGetLastError());
@@ -780,6 +902,8 @@ pa_status pa_align_batch_device(pa_ctx *ctx, const pa_config *config, const uint
 {
     if (!ctx) return PA_ERR_INVALID_ARGUMENT;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, PA_ERR_CUDA, "cudaSetDevice");
+    // sequence lengths are on the device: CTA mode covers sequence1 up to the default ring
+    ctx->want_ring_m = std::max<int64_t>(ctx->ring_m, kDefaultRingM);
     cudaStream_t user = (cudaStream_t)stream;
     if (user && user != ctx->stream) {
         // order the context stream after the caller's work, and the caller's after ours
@@ -817,6 +941,15 @@ pa_status pa_align_batch_banded(pa_ctx *ctx, const pa_config *config, const uint
     pa_config cfg = *config;
     cfg.band_mode = 1;
     return align_host(ctx, &cfg, seq1, off1, seq2, off2, n_pairs, out, stats, bands);
+}
+
+pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    ctx->long_cells = cells > (uint64_t)INT64_MAX ? INT64_MAX : (int64_t)std::max<uint64_t>(cells, 1);
+    for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);   // the classifier's rule changed
+    ctx->graphs.clear();
+    return PA_OK;
 }
 
 pa_status pa_set_band_options(pa_ctx *ctx, const pa_band_options *o)
@@ -881,9 +1014,14 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
         return s;
     }
     if (!seq1 || !off1 || !seq2 || !off2 || !out) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null buffer");
-    for (uint64_t k = 0; k < n_pairs; ++k)
+    int64_t long_m = 0;
+    for (uint64_t k = 0; k < n_pairs; ++k) {
         if (off1[k + 1] < off1[k] || off2[k + 1] < off2[k])
             return fail(ctx, PA_ERR_INVALID_ARGUMENT, "offsets must be non-decreasing");
+        const int64_t m = (int64_t)(off1[k + 1] - off1[k]), n = (int64_t)(off2[k + 1] - off2[k]);
+        if (m * n >= ctx->long_cells) long_m = std::max(long_m, m);
+    }
+    ctx->want_ring_m = long_m;      // exact: the ring rows hold the longest CTA-mode sequence1
     if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, PA_ERR_CUDA, "cudaSetDevice");
     // the device copies hold bytes [0, off[n]) with offsets rebased to 0
     const uint64_t base1 = off1[0], base2 = off2[0];
@@ -918,29 +1056,7 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
     if (s) return s;
     PA_CUDA(ctx, cudaMemcpyAsync(out, ctx->in_out.p, n_pairs * sizeof(pa_result), cudaMemcpyDeviceToHost, st));
     PA_CUDA(ctx, cudaStreamSynchronize(st));
-    if (stats) {
-        PrepStats ps;
-        uint32_t ctr[8];
-        PA_CUDA(ctx, cudaMemcpy(&ps, ctx->pstats.p, sizeof(ps), cudaMemcpyDeviceToHost));
-        PA_CUDA(ctx, cudaMemcpy(ctr, ctx->counters.p, sizeof(ctr), cudaMemcpyDeviceToHost));
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-        stats->device_ms = ms;
-        if (cudaEventElapsedTime(&ms, ctx->ev_dp0, ctx->ev_dp1) == cudaSuccess) stats->dp_ms = ms;
-        cudaGetLastError();
-        stats->cells = ps.cells;
-        stats->pairs_s16 = ps.n_class[K_S16] - ctr[4];
-        stats->pairs_s32 = ps.n_class[K_S32] + ctr[4];
-        stats->pairs_general = ps.n_class[K_GEN];
-        stats->pairs_trivial = ps.n_class[K_NONE];
-        stats->pairs_rerun = ctr[4];
-        if (ps.overflow) return fail(ctx, PA_ERR_OVERFLOW, "scores of some pairs could exceed int32");
-    } else {
-        PrepStats ps;
-        PA_CUDA(ctx, cudaMemcpy(&ps, ctx->pstats.p, sizeof(ps), cudaMemcpyDeviceToHost));
-        if (ps.overflow) return fail(ctx, PA_ERR_OVERFLOW, "scores of some pairs could exceed int32");
-    }
-    return PA_OK;
+    return read_stats(ctx, stats);
 }
 
 pa_status pa_align_one_to_many(pa_ctx *ctx, const pa_config *config, const uint8_t *query, uint64_t query_len,
@@ -1006,7 +1122,8 @@ pa_status pa_band_labels(pa_ctx *ctx, const pa_config *config, const uint8_t *se
         return fail(ctx, PA_ERR_OUT_OF_MEMORY, "band labels: cudaMalloc failed");
     }
     cudaStream_t st = ctx->stream;
-    bool ok = cudaMemcpyAsync(d1, seq1 + off1[0], b1, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+    bool ok = cudaMemsetAsync(dctr, 0, 64, st) == cudaSuccess &&
+              cudaMemcpyAsync(d1, seq1 + off1[0], b1, cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaMemcpyAsync(d2, seq2 + off2[0], b2, cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaMemcpyAsync(dr1, r1.data(), b1, cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaMemcpyAsync(dr2, r2.data(), b2, cudaMemcpyHostToDevice, st) == cudaSuccess &&
@@ -1014,11 +1131,20 @@ pa_status pa_band_labels(pa_ctx *ctx, const pa_config *config, const uint8_t *se
               cudaMemcpyAsync(do2, o2.data(), 8 * (n_pairs + 1), cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaMemsetAsync(dlab, 0, sizeof(int32_t) * 8 * n_pairs, st) == cudaSuccess;
     const int grid = band_labels_occupancy() * ctx->sm_count;
+    // long pairs go to the CTA-mode labeller (whole blocks per pair, ring rows per block)
+    int64_t long_m = 0;
+    for (uint64_t k = 0; k < n_pairs; ++k) {
+        const int64_t m = (int64_t)(o1[k + 1] - o1[k]), n = (int64_t)(o2[k + 1] - o2[k]);
+        if (m * n >= ctx->long_cells && m <= (1 << 20) && n <= (1 << 20)) long_m = std::max(long_m, m);
+    }
+    if (ok && long_m && ensure_ring(ctx, long_m) != PA_OK) ok = false;
+    const int64_t ring_m = ctx->ring.p ? ctx->ring_m : 0;
     std::vector<uint64_t> doff(n_pairs, 0);
     std::vector<uint32_t> order;
     uint64_t k = 0;
     while (ok && k < n_pairs) {
         order.clear();
+        std::vector<uint32_t> longs;
         uint64_t used = 0;
         for (; k < n_pairs; ++k) {
             const uint64_t m = o1[k + 1] - o1[k], n = o2[k + 1] - o2[k];
@@ -1028,10 +1154,13 @@ pa_status pa_band_labels(pa_ctx *ctx, const pa_config *config, const uint8_t *se
             if (used + need > kDumpBudget) break;
             doff[k] = used;
             used += need;
-            order.push_back((uint32_t)k);
+            const bool lng = (int64_t)(m * n) >= ctx->long_cells && (int64_t)m <= ring_m && n <= (1u << 20);
+            (lng ? longs : order).push_back((uint32_t)k);
         }
-        if (!ok || order.empty()) break;
-        const uint32_t ctr[2] = {0u, (uint32_t)order.size()};   // begin, count
+        if (!ok || (order.empty() && longs.empty())) break;
+        const uint32_t ns = (uint32_t)order.size();
+        order.insert(order.end(), longs.begin(), longs.end());
+        const uint32_t ctr[4] = {0u, ns, ns, (uint32_t)longs.size()};   // begin, count per list
         ok = cudaMemcpyAsync(ddoff, doff.data(), 8 * n_pairs, cudaMemcpyHostToDevice, st) == cudaSuccess &&
              cudaMemcpyAsync(dorder, order.data(), 4 * order.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
              cudaMemcpyAsync(dctr + 8, ctr, sizeof(ctr), cudaMemcpyHostToDevice, st) == cudaSuccess;
@@ -1042,12 +1171,21 @@ pa_status pa_band_labels(pa_ctx *ctx, const pa_config *config, const uint8_t *se
             L.order = dorder; L.begin_ptr = dctr + 8; L.count_ptr = dctr + 9; L.unit_counter = dctr;
             L.out = dout; L.boundary = dbound; L.G = 8;
             L.dump = ddump; L.dump_off = ddoff; L.labels = dlab;
-            ok = cudaMemsetAsync(dctr, 0, 4, st) == cudaSuccess;
-            if (ok) band_labels_launch(rev == 1, grid, st, L, P);
+            L.error = dctr + 4;
+            ok = cudaMemsetAsync(dctr, 0, 8, st) == cudaSuccess;
+            if (ok && ns) band_labels_launch(rev == 1, grid, st, L, P);
+            if (ok && !longs.empty()) {
+                L.begin_ptr = dctr + 10; L.count_ptr = dctr + 11; L.unit_counter = dctr + 1; L.G = 32;
+                L.ring = (Cell *)ctx->ring.p;
+                L.ring_stride = (uint64_t)ctx->ring_m + 2;
+                band_labels_cta_launch(rev == 1, ctx->ring_grid, st, L, P);
+            }
             ok = ok && cudaGetLastError() == cudaSuccess;
         }
         ok = ok && cudaStreamSynchronize(st) == cudaSuccess;      // the host staging arrays are reused
     }
+    uint32_t err_bits = 0;
+    if (ok && (cudaMemcpy(&err_bits, dctr + 4, 4, cudaMemcpyDeviceToHost) != cudaSuccess || err_bits)) ok = false;
     ok = ok && cudaMemcpyAsync(labels, dlab, sizeof(int32_t) * 8 * n_pairs, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
          cudaStreamSynchronize(st) == cudaSuccess;
     cleanup();

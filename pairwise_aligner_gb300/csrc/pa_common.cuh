@@ -19,9 +19,12 @@ struct DpParams {
 };
 
 // Work classes produced by the classifier; the class is the top field of the bucket key.
-enum Klass : uint32_t { K_S16 = 0, K_S32 = 1, K_GEN = 2, K_NONE = 3 };
+// Classes 4..6 are the long-pair versions of 0..2, computed by whole blocks (CTA mode).
+enum Klass : uint32_t { K_S16 = 0, K_S32 = 1, K_GEN = 2, K_NONE = 3, K_S16L = 4, K_S32L = 5, K_GENL = 6 };
+constexpr int kClasses = 7;
+constexpr uint32_t kLongOffset = 4;
 
-constexpr int kKeyBits = 18;                 // 2 class | 6 pass | 10 length bits
+constexpr int kKeyBits = 19;                 // 3 class | 6 pass | 10 length bits
 constexpr uint32_t kBuckets = 1u << kKeyBits;
 constexpr int kClassShift = 16;
 
@@ -71,6 +74,10 @@ struct DpLaunch {
     int32_t *band_ub;             // optional: the largest exit bound per pair
     int32_t band_rows;            // rows per pass of the window table (G * R)
     int32_t band_round;
+    // CTA mode (long pairs): each block owns ring rows of ring_stride cells, one per group
+    Cell *ring;
+    uint64_t ring_stride;
+    uint32_t *error;              // error bits (kErrWaitTimeout), may be null
 };
 
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)

@@ -41,6 +41,8 @@
 //   global -- H(m, n) is read where it is computed; free trailing gaps also
 //             scan the last row (i = m) and the last column (j = n).
 #pragma once
+#include <cuda/atomic>
+
 #include "pa_common.cuh"
 
 namespace pa {
@@ -145,7 +147,11 @@ struct GroupWork {
     int32_t Kt, clampt;        // the same as true-score integers
     int32_t floor_true;        // global s16 lanes: true value of the clamp
     const uint32_t *qt[2];
-    Cell *buf;
+    Cell *buf;                     // single-group passes read and write this boundary row
+    Cell *bin, *bout;              // the boundary row a pass reads (from the pass above) and writes
+    int *prog_in, *prog_out;       // CTA mode: progress of the pass above / of this pass
+    int32_t base_in, base_out;     // progress value of column 0 of those passes
+    int32_t seen;                  // last progress value thread 0 observed
     int32_t cs[2], ci[2], cj[2];   // candidate (score, end1, end2) per lane
     int32_t lb_v[8], lb_j[8];      // label mode: best forward + reverse score per checkpoint and its row
     // band mode: columns ibase+1 .. iend of the current pass; thread 0's first diagonal
@@ -154,6 +160,30 @@ struct GroupWork {
     int32_t ub[2];                 // largest bound on a path that leaves the band, per lane
     unsigned long long cells;      // band cells computed (statistics)
 };
+
+// CTA mode: the groups of a block work on consecutive passes of one pair; the
+// group of pass p waits (thread 0, before reading boundary column c) until the
+// pass above has published column c.  Waits are bounded; a wait that runs out
+// sets an error bit and the kernel carries on (its result is reported invalid).
+constexpr uint32_t kSpinLimit = 1u << 24;
+constexpr uint32_t kErrWaitTimeout = 1u;
+
+__device__ __forceinline__ int32_t wait_progress(int *flag, int32_t need, uint32_t *err)
+{
+    cuda::atomic_ref<int, cuda::thread_scope_block> a(*flag);
+    for (uint32_t it = 0; it < kSpinLimit; ++it) {
+        const int v = a.load(cuda::memory_order_acquire);
+        if (v >= need) return v;
+        if (it >= 64) __nanosleep(64);
+    }
+    if (err) atomicOr(err, kErrWaitTimeout);
+    return INT32_MAX;
+}
+
+__device__ __forceinline__ void publish_progress(int *flag, int32_t v)
+{
+    cuda::atomic_ref<int, cuda::thread_scope_block>(*flag).store(v, cuda::memory_order_release);
+}
 
 // Upper bound on the score of a path that enters cell (i, j) from inside the band
 // and then runs to (m, n): `gapv` is the score of entering in a gap state, `diagv`
@@ -183,7 +213,7 @@ __device__ __forceinline__ uint32_t stored(const GroupWork &w, int32_t true_valu
 
 // VAR bit 0: short-chain form of the vertical gap; bit 2: branch-free top input for
 // thread 0 and an L1 prefetch of the score tables eight columns ahead.
-template <class V, int R, int RA, int MODE, bool GEN, int VAR>
+template <class V, int R, int RA, int MODE, bool GEN, int VAR, bool SYNC = false>
 __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, GroupWork &w, int p, int t, int G,
                                          unsigned gmask, uint4 *snap)
 {
@@ -245,7 +275,15 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
         }
     };
     Cell nbuf = Cell{0u, 0u};                        // thread 0, pass > 0: next boundary cell
-    if (t == 0 && p > 0) nbuf = w.buf[ibase + 1];
+    // thread 0 of a pass below the first reads the boundary row; in CTA mode it first
+    // waits until the pass above has published the column
+    auto ready = [&](int32_t col) {
+        if (SYNC && w.seen < w.base_in + col) w.seen = wait_progress(w.prog_in, w.base_in + col, L.error);
+    };
+    if (t == 0 && p > 0) {
+        ready(ibase + 1);
+        nbuf = w.bin[ibase + 1];
+    }
     constexpr bool TUNED = (VAR & 4) != 0;
     const bool first_thread = t == 0;
     const bool top_border = first_thread && p == 0;
@@ -259,7 +297,10 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             const uint32_t nt = V::max2(V::subc(topH, i == 1 ? step1 : stepn), CLAMP);
             topH = top_border ? nt : topH;
             const Cell c = nbuf;
-            if (top_buffer && i < iend) nbuf = w.buf[i + 1];
+            if (top_buffer && i < iend) {
+                ready(i + 1);
+                nbuf = w.bin[i + 1];
+            }
             upH = top_border ? nt : (top_buffer ? c.h : upH);
             upE = top_border ? V::subc(nt, GOEA) : (top_buffer ? c.e : upE);
             if (!GEN && i + 8 <= iend) {
@@ -274,7 +315,10 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             } else {
                 upH = nbuf.h;
                 upE = nbuf.e;
-                if (i < iend) nbuf = w.buf[i + 1];
+                if (i < iend) {
+                    ready(i + 1);
+                    nbuf = w.bin[i + 1];
+                }
             }
         }
         if (BAND && i == iend) top_last = upH;
@@ -317,7 +361,10 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
         prevH = upH;
         outH = H[RA - 1];
         outE = Ed;
-        if (t == G - 1 && !last_pass) w.buf[i] = Cell{outH, outE};
+        if (t == G - 1 && !last_pass) {
+            w.bout[i] = Cell{outH, outE};
+            if (SYNC && ((i & 7) == 0 || i == iend)) publish_progress(w.prog_out, w.base_out + i);
+        }
 
         if (MODE == M_LABEL_FWD || MODE == M_LABEL_REV) {
             // forward: keep the checkpoint columns; reverse (sequences reversed): column i is
@@ -447,7 +494,236 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
     }
 }
 
+// ---- pieces shared by the single-group and the CTA kernels ---------------------------
+
+// The work of pair order[first] (and order[first + 1] in s16x2 lanes).
+template <class V, int MODE>
+__device__ __forceinline__ void init_work(const DpLaunch &L, const DpParams &P, const uint32_t *order, uint32_t first,
+                                          uint32_t count, int G, int R, GroupWork &w)
+{
+    constexpr int NL = V::LANES;
+    w.id[0] = order[first];
+    w.has_b = NL == 2 && first + 1 < count;
+    w.id[1] = w.has_b ? order[first + 1] : w.id[0];
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        w.qoff[l] = L.off1[w.id[l]];
+        w.m[l] = (int32_t)(L.off1[w.id[l] + 1] - w.qoff[l]);
+        w.toff[l] = L.off2[w.id[l]];
+        w.n[l] = (int32_t)(L.off2[w.id[l] + 1] - w.toff[l]);
+        w.qt[l] = L.qtab + w.qoff[l] + w.id[l];
+        w.cs[l] = MODE == M_LOCAL ? 0 : INT32_MIN;
+        w.ci[l] = 0;
+        w.cj[l] = 0;
+    }
+    for (int c = 0; c < 8; ++c) { w.lb_v[c] = INT32_MIN; w.lb_j[c] = 0; }
+    w.ub[0] = w.ub[1] = INT32_MIN;
+    w.cells = 0;
+    w.ms = NL == 2 ? max(w.m[0], w.m[1]) : w.m[0];
+    w.nh = NL == 2 ? max(w.n[0], w.n[1]) : w.n[0];
+    w.rows_full = G * R;
+    w.passes = (w.nh + w.rows_full - 1) / w.rows_full;
+    const uint32_t owner = (NL == 2 && w.m[1] > w.m[0]) ? w.id[1] : w.id[0];
+    w.buf = L.boundary + (L.off1[owner] + owner);
+    w.bin = w.bout = w.buf;
+    w.seen = INT32_MIN;
+    if (NL == 2) {
+        if (MODE == M_LOCAL) {
+            w.Kt = 2048;
+            w.clampt = 2048;
+            w.floor_true = 0;
+        } else {
+            const int32_t ub = P.smax * max(min(w.m[0], w.n[0]), min(w.m[1], w.n[1]));
+            w.Kt = 32767 - 512 - ub;
+            w.clampt = 2048;
+            w.floor_true = 2048 - w.Kt;
+        }
+        w.K = V::splat(w.Kt);
+        w.CLAMP = V::splat(w.clampt);
+    } else {
+        w.Kt = 0;
+        w.clampt = MODE == M_LOCAL ? 0 : INT32_MIN;
+        w.floor_true = INT32_MIN;
+        w.K = 0;
+        w.CLAMP = (uint32_t)w.clampt;
+    }
+}
+
+// Band mode: the column window of pass p, the union of the lanes' windows from the
+// window table (monotone and overlapping per lane; a lane past its last pass keeps
+// its last window, which ends at its column m, so the union is too).
+template <int NL>
+__device__ __forceinline__ int2 band_window(const DpLaunch &L, const GroupWork &w, int p)
+{
+    int32_t a = INT32_MAX, b = 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+        if (l == 1 && !w.has_b) continue;
+        const int32_t pl = (w.n[l] + w.rows_full - 1) / w.rows_full;
+        const uint64_t slot = (L.off2[w.id[l]] - L.off2[0]) / (uint64_t)L.band_rows + w.id[l];
+        const int2 x = L.band_win[slot + min(p, pl - 1)];
+        a = min(a, x.x);
+        b = max(b, x.y);
+    }
+    if (a == INT32_MAX) { a = 1; b = w.ms; }
+    a = p == 0 ? 1 : max(a, 1);
+    b = min(max(b, a), w.ms);
+    return make_int2(a, b);
+}
+
+// One pass p of the group's pair(s): the band window and its exits (band mode),
+// then the wavefront sweep.
+template <class V, int R, int MODE, bool GEN, int VAR, bool SYNC>
+__device__ __forceinline__ void pass_body(const DpLaunch &L, const DpParams &P, GroupWork &w, int p, int t, int G,
+                                          unsigned gmask, uint4 *snap)
+{
+    constexpr int NL = V::LANES;
+    const int32_t rem = w.nh - p * w.rows_full;
+    const int32_t rpt = rem >= w.rows_full ? R : ((rem + G * kChunk - 1) / (G * kChunk)) * kChunk;
+    const uint32_t NEGV = NL == 2 ? w.CLAMP : (uint32_t)kNeg32;
+    int2 bprev = make_int2(1, w.ms), bcur = bprev, bnext = bprev;
+    const bool more = p + 1 < w.passes;
+    if (MODE == M_BAND) {
+        bcur = band_window<NL>(L, w, p);
+        if (p > 0) bprev = band_window<NL>(L, w, p - 1);
+        if (more) bnext = band_window<NL>(L, w, p + 1);
+        // the exits below assume monotone, overlapping windows: refuse to certify otherwise
+        if (p > 0 && (bcur.x < bprev.x || bcur.y < bprev.y || bcur.x > bprev.y)) w.ub[0] = w.ub[1] = INT32_MAX;
+        w.ibase = bcur.x - 1;
+        w.iend = bcur.y;
+        const int32_t c0 = bcur.x - 1;
+        w.diag0 = NEGV;
+        if (t == 0 && p > 0 && c0 >= bprev.x && c0 <= bprev.y) {
+            if (SYNC && w.seen < w.base_in + c0) w.seen = wait_progress(w.prog_in, w.base_in + c0, L.error);
+            w.diag0 = w.bin[c0].h;
+        }
+    }
+    switch (rpt / kChunk) {
+    case 1: run_pass<V, R, 4, MODE, GEN, VAR, SYNC>(L, P, w, p, t, G, gmask, snap); break;
+    case 2: run_pass<V, R, 8, MODE, GEN, VAR, SYNC>(L, P, w, p, t, G, gmask, snap); break;
+    case 3: run_pass<V, R, 12, MODE, GEN, VAR, SYNC>(L, P, w, p, t, G, gmask, snap); break;
+    default: run_pass<V, R, R, MODE, GEN, VAR, SYNC>(L, P, w, p, t, G, gmask, snap); break;
+    }
+    __syncwarp(gmask);
+    if (MODE == M_BAND) {
+        const int32_t jlo = p * w.rows_full + 1, jhi = p * w.rows_full + G * rpt;
+        const int32_t goe = P.gap_open + P.gap_ext;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
+            if (l == 1 && !w.has_b) continue;
+            const int32_t ml = w.m[l], nl = w.n[l];
+            if (jlo > nl) continue;
+            if (t == 0) w.cells += (unsigned long long)(bcur.y - bcur.x + 1) * (min(jhi, nl) - jlo + 1);
+            if (p == 0)       // along the top border past the window, then down into row 1
+                for (int32_t i = bcur.y + 1 + t; i <= ml; i += G)
+                    w.ub[l] = max(w.ub[l], exit_bound(P, border(P, 0, i) + goe, border(P, 0, i - 1) + P.smax,
+                                                      i, 1, ml, nl));
+            if (bcur.x > 1)   // down the left border, then into column 1 of this pass
+                for (int32_t j = jlo + t; j <= min(jhi, nl); j += G)
+                    w.ub[l] = max(w.ub[l], exit_bound(P, border(P, 0, j) + goe, border(P, 0, j - 1) + P.smax,
+                                                      1, j, ml, nl));
+            if (more && jhi < nl) {   // through the bottom edge left of the next window
+                const int32_t last = min(min(bcur.y, bnext.x - 1), ml);
+                for (int32_t i = bcur.x + t; i <= last; i += G) {
+                    const Cell c = w.bout[i];
+                    w.ub[l] = max(w.ub[l], exit_bound(P, V::get(c.e, l) - w.Kt, kNeg32, i, jhi + 1, ml, nl));
+                    if (i + 1 < bnext.x)
+                        w.ub[l] = max(w.ub[l], exit_bound(P, kNeg32, V::get(c.h, l) - w.Kt + P.smax, i + 1,
+                                                          jhi + 1, ml, nl));
+                }
+            }
+        }
+        if (more)             // columns the next pass reads beyond this window: outside
+            for (int32_t i = bcur.y + 1 + t; i <= bnext.y; i += G) w.bout[i] = Cell{NEGV, NEGV};
+        __syncwarp(gmask);
+    }
+}
+
+// Reduction over the threads of a group (results in every thread).
+template <class V, int MODE>
+__device__ __forceinline__ void reduce_group(GroupWork &w, unsigned gmask, int G)
+{
+    constexpr int NL = V::LANES;
+    if (MODE == M_LABEL_REV)
+        for (int c = 0; c < 8; ++c)
+            for (int off = G >> 1; off >= 1; off >>= 1) {
+                const int32_t ov = __shfl_xor_sync(gmask, w.lb_v[c], off, G);
+                const int32_t oj = __shfl_xor_sync(gmask, w.lb_j[c], off, G);
+                if (ov > w.lb_v[c] || (ov == w.lb_v[c] && oj < w.lb_j[c])) { w.lb_v[c] = ov; w.lb_j[c] = oj; }
+            }
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+        if (MODE == M_BAND)
+            for (int off = G >> 1; off >= 1; off >>= 1) w.ub[l] = max(w.ub[l], __shfl_xor_sync(gmask, w.ub[l], off, G));
+        for (int off = G >> 1; off >= 1; off >>= 1) {
+            const int32_t os = __shfl_xor_sync(gmask, w.cs[l], off, G);
+            const int32_t oi = __shfl_xor_sync(gmask, w.ci[l], off, G);
+            const int32_t oj = __shfl_xor_sync(gmask, w.cj[l], off, G);
+            if (better(os, oi, oj, w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = os; w.ci[l] = oi; w.cj[l] = oj; }
+        }
+    }
+}
+
+// Results of the unit (one thread): labels, free-end borders, the s16 exactness
+// check, the band outcome.
+template <class V, int MODE>
+__device__ __forceinline__ void emit(const DpLaunch &L, const DpParams &P, GroupWork &w, uint32_t first)
+{
+    constexpr int NL = V::LANES;
+    if (MODE == M_LABEL_REV)
+        for (int c = 0; c < 8; ++c) L.labels[(uint64_t)w.id[0] * 8 + c] = w.lb_j[c] - checkpoint_col(c, w.m[0]);
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+        if (l == 1 && !w.has_b) continue;
+        if (MODE == M_GLOBAL_FREE) {
+            if (P.last_column_free) {            // H(0, n)
+                const int32_t x = border(P, P.first_row_free, w.n[l]);
+                if (better(x, 0, w.n[l], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = x; w.ci[l] = 0; w.cj[l] = w.n[l]; }
+            }
+            if (P.last_row_free) {               // H(m, 0)
+                const int32_t x = border(P, P.first_column_free, w.m[l]);
+                if (better(x, w.m[l], 0, w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = x; w.ci[l] = w.m[l]; w.cj[l] = 0; }
+            }
+        }
+        pa_result r;
+        r.score = w.cs[l];
+        r.end1 = w.ci[l];
+        r.end2 = w.cj[l];
+        r.width = V::WIDTH;
+        r.flags = L.rerun ? PA_RESULT_RERUN : 0;
+        r.band_rounds = 0;
+        if (MODE == M_LOCAL && w.cs[l] <= 0) { r.end1 = 0; r.end2 = 0; }
+        if (MODE == M_BAND) {
+            uint8_t code;
+            if (NL == 2 && (int64_t)w.cs[l] <= (int64_t)w.floor_true + (int64_t)P.smax * min(w.m[l], w.n[l])) {
+                code = 3;                           // a clamp may have reached it: redo in s32
+            } else if (w.cs[l] != INT32_MIN && w.ub[l] <= w.cs[l]) {   // no path leaving the band scores more
+                r.flags |= PA_RESULT_BANDED;
+                r.band_rounds = (uint16_t)L.band_round;
+                L.out[w.id[l]] = r;
+                code = 0;
+            } else {
+                code = 1;
+            }
+            L.band_code[first + l] = code;
+            if (L.band_ub) L.band_ub[w.id[l]] = w.ub[l];
+            continue;
+        }
+        if (NL == 2 && MODE != M_LOCAL &&
+            (int64_t)w.cs[l] <= (int64_t)w.floor_true + (int64_t)P.smax * min(w.m[l], w.n[l])) {
+            // a clamp may have reached this result: recompute the pair in s32
+            const uint32_t slot = atomicAdd(L.rerun_count, 1u);
+            L.rerun_list[slot] = w.id[l];
+            continue;
+        }
+        L.out[w.id[l]] = r;
+    }
+    if (MODE == M_BAND && L.dp_cells && w.cells) atomicAdd(L.dp_cells, w.cells);
+}
+
 // GEN = byte-compare scoring (any bytes, any int32 scores), always with L32 lanes.
+// One group of G lanes per pair (two pairs in s16x2 lanes); the group runs all
+// passes of its pair(s) one after the other.
 template <class V, int R, int MODE, bool GEN, int VAR, int MINB = 2>
 __global__ void __launch_bounds__(kBlock, MINB) dp_kernel(DpLaunch L, DpParams P)
 {
@@ -472,201 +748,94 @@ __global__ void __launch_bounds__(kBlock, MINB) dp_kernel(DpLaunch L, DpParams P
         u = n_units - 1 - u;                         // largest shapes first
         const uint32_t first = u * ppw + (uint32_t)g * NL;
         if (first >= count) continue;                // idle group in the last unit
-
         GroupWork w;
-        w.id[0] = order[first];
-        w.has_b = NL == 2 && first + 1 < count;
-        w.id[1] = w.has_b ? order[first + 1] : w.id[0];
-#pragma unroll
-        for (int l = 0; l < 2; ++l) {
-            w.qoff[l] = L.off1[w.id[l]];
-            w.m[l] = (int32_t)(L.off1[w.id[l] + 1] - w.qoff[l]);
-            w.toff[l] = L.off2[w.id[l]];
-            w.n[l] = (int32_t)(L.off2[w.id[l] + 1] - w.toff[l]);
-            w.qt[l] = L.qtab + w.qoff[l] + w.id[l];
-            w.cs[l] = MODE == M_LOCAL ? 0 : INT32_MIN;
-            w.ci[l] = 0;
-            w.cj[l] = 0;
-        }
-        for (int c = 0; c < 8; ++c) { w.lb_v[c] = INT32_MIN; w.lb_j[c] = 0; }
-        w.ub[0] = w.ub[1] = INT32_MIN;
-        w.cells = 0;
-        w.ms = NL == 2 ? max(w.m[0], w.m[1]) : w.m[0];
-        w.nh = NL == 2 ? max(w.n[0], w.n[1]) : w.n[0];
-        w.rows_full = G * R;
-        w.passes = (w.nh + w.rows_full - 1) / w.rows_full;
-        const uint32_t owner = (NL == 2 && w.m[1] > w.m[0]) ? w.id[1] : w.id[0];
-        w.buf = L.boundary + (L.off1[owner] + owner);
-        if (NL == 2) {
-            if (MODE == M_LOCAL) {
-                w.Kt = 2048;
-                w.clampt = 2048;
-                w.floor_true = 0;
-            } else {
-                const int32_t ub = P.smax * max(min(w.m[0], w.n[0]), min(w.m[1], w.n[1]));
-                w.Kt = 32767 - 512 - ub;
-                w.clampt = 2048;
-                w.floor_true = 2048 - w.Kt;
-            }
-            w.K = V::splat(w.Kt);
-            w.CLAMP = V::splat(w.clampt);
-        } else {
-            w.Kt = 0;
-            w.clampt = MODE == M_LOCAL ? 0 : INT32_MIN;
-            w.floor_true = INT32_MIN;
-            w.K = 0;
-            w.CLAMP = (uint32_t)w.clampt;
-        }
-
-        // band mode: the column window of each pass is the union of the lanes' windows,
-        // kept monotone and overlapping the previous pass by at least one column
-        int2 bcur = make_int2(1, w.ms), bprev = make_int2(1, w.ms);
-        auto band_window = [&](int p, int2 prev) -> int2 {
-            int32_t a = INT32_MAX, b = 0;
-#pragma unroll
-            for (int l = 0; l < NL; ++l) {
-                if (l == 1 && !w.has_b) continue;
-                if ((int64_t)p * w.rows_full >= w.n[l]) continue;
-                const uint64_t slot = (L.off2[w.id[l]] - L.off2[0]) / (uint64_t)L.band_rows + w.id[l];
-                const int2 x = L.band_win[slot + p];
-                a = min(a, x.x);
-                b = max(b, x.y);
-            }
-            if (a == INT32_MAX) { a = 1; b = w.ms; }
-            if (p > 0) { a = max(min(a, prev.y), prev.x); b = max(b, prev.y); }
-            a = p == 0 ? 1 : max(a, 1);
-            b = min(max(b, a), w.ms);
-            return make_int2(a, b);
-        };
-        const uint32_t NEGV = MODE == M_BAND ? (NL == 2 ? w.CLAMP : (uint32_t)kNeg32) : 0u;
-        if (MODE == M_BAND) bcur = band_window(0, bprev);
-
-        for (int p = 0; p < w.passes; ++p) {
-            const int32_t rem = w.nh - p * w.rows_full;
-            const int32_t rpt = rem >= w.rows_full ? R : ((rem + G * kChunk - 1) / (G * kChunk)) * kChunk;
-            if (MODE == M_BAND) {
-                w.ibase = bcur.x - 1;
-                w.iend = bcur.y;
-                const int32_t c0 = bcur.x - 1;
-                w.diag0 = (p > 0 && c0 >= bprev.x && c0 <= bprev.y) ? w.buf[c0].h : NEGV;
-            }
-            switch (rpt / kChunk) {
-            case 1: run_pass<V, R, 4, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
-            case 2: run_pass<V, R, 8, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
-            case 3: run_pass<V, R, 12, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
-            default: run_pass<V, R, R, MODE, GEN, VAR>(L, P, w, p, t, G, gmask, snap_store); break;
-            }
-            __syncwarp(gmask);
-            if (MODE == M_BAND) {
-                const bool more = p + 1 < w.passes;
-                const int2 bnext = more ? band_window(p + 1, bcur) : bcur;
-                const int32_t jlo = p * w.rows_full + 1, jhi = p * w.rows_full + G * rpt;
-                const int32_t goe = P.gap_open + P.gap_ext;
-#pragma unroll
-                for (int l = 0; l < NL; ++l) {
-                    if (l == 1 && !w.has_b) continue;
-                    const int32_t ml = w.m[l], nl = w.n[l];
-                    if (jlo > nl) continue;
-                    if (t == 0) w.cells += (unsigned long long)(bcur.y - bcur.x + 1) * (min(jhi, nl) - jlo + 1);
-                    if (p == 0)       // along the top border past the window, then down into row 1
-                        for (int32_t i = bcur.y + 1 + t; i <= ml; i += G)
-                            w.ub[l] = max(w.ub[l], exit_bound(P, border(P, 0, i) + goe, border(P, 0, i - 1) + P.smax,
-                                                              i, 1, ml, nl));
-                    if (bcur.x > 1)   // down the left border, then into column 1 of this pass
-                        for (int32_t j = jlo + t; j <= min(jhi, nl); j += G)
-                            w.ub[l] = max(w.ub[l], exit_bound(P, border(P, 0, j) + goe, border(P, 0, j - 1) + P.smax,
-                                                              1, j, ml, nl));
-                    if (more && jhi < nl) {   // through the bottom edge left of the next window
-                        const int32_t last = min(min(bcur.y, bnext.x - 1), ml);
-                        for (int32_t i = bcur.x + t; i <= last; i += G) {
-                            const Cell c = w.buf[i];
-                            w.ub[l] = max(w.ub[l], exit_bound(P, V::get(c.e, l) - w.Kt, kNeg32, i, jhi + 1, ml, nl));
-                            if (i + 1 < bnext.x)
-                                w.ub[l] = max(w.ub[l], exit_bound(P, kNeg32, V::get(c.h, l) - w.Kt + P.smax, i + 1,
-                                                                  jhi + 1, ml, nl));
-                        }
-                    }
-                }
-                if (more)             // columns the next pass reads beyond this window: outside
-                    for (int32_t i = bcur.y + 1 + t; i <= bnext.y; i += G) w.buf[i] = Cell{NEGV, NEGV};
-                __syncwarp(gmask);
-                bprev = bcur;
-                bcur = bnext;
-            }
-        }
-
-        if (MODE == M_LABEL_REV) {
-            for (int c = 0; c < 8; ++c) {
-                for (int off = G >> 1; off >= 1; off >>= 1) {
-                    const int32_t ov = __shfl_xor_sync(gmask, w.lb_v[c], off, G);
-                    const int32_t oj = __shfl_xor_sync(gmask, w.lb_j[c], off, G);
-                    if (ov > w.lb_v[c] || (ov == w.lb_v[c] && oj < w.lb_j[c])) { w.lb_v[c] = ov; w.lb_j[c] = oj; }
-                }
-                if (t == 0) L.labels[(uint64_t)w.id[0] * 8 + c] = w.lb_j[c] - checkpoint_col(c, w.m[0]);
-            }
-        }
-        // group reduction of the candidates
-#pragma unroll
-        for (int l = 0; l < NL; ++l) {
-            if (MODE == M_BAND)
-                for (int off = G >> 1; off >= 1; off >>= 1) w.ub[l] = max(w.ub[l], __shfl_xor_sync(gmask, w.ub[l], off, G));
-            for (int off = G >> 1; off >= 1; off >>= 1) {
-                const int32_t os = __shfl_xor_sync(gmask, w.cs[l], off, G);
-                const int32_t oi = __shfl_xor_sync(gmask, w.ci[l], off, G);
-                const int32_t oj = __shfl_xor_sync(gmask, w.cj[l], off, G);
-                if (better(os, oi, oj, w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = os; w.ci[l] = oi; w.cj[l] = oj; }
-            }
-        }
-        if (t == 0) {
-#pragma unroll
-            for (int l = 0; l < NL; ++l) {
-                if (l == 1 && !w.has_b) continue;
-                if (MODE == M_GLOBAL_FREE) {
-                    if (P.last_column_free) {            // H(0, n)
-                        const int32_t x = border(P, P.first_row_free, w.n[l]);
-                        if (better(x, 0, w.n[l], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = x; w.ci[l] = 0; w.cj[l] = w.n[l]; }
-                    }
-                    if (P.last_row_free) {               // H(m, 0)
-                        const int32_t x = border(P, P.first_column_free, w.m[l]);
-                        if (better(x, w.m[l], 0, w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = x; w.ci[l] = w.m[l]; w.cj[l] = 0; }
-                    }
-                }
-                pa_result r;
-                r.score = w.cs[l];
-                r.end1 = w.ci[l];
-                r.end2 = w.cj[l];
-                r.width = V::WIDTH;
-                r.flags = L.rerun ? PA_RESULT_RERUN : 0;
-                r.band_rounds = 0;
-                if (MODE == M_LOCAL && w.cs[l] <= 0) { r.end1 = 0; r.end2 = 0; }
-                if (MODE == M_BAND) {
-                    uint8_t code;
-                    if (NL == 2 && (int64_t)w.cs[l] <= (int64_t)w.floor_true + (int64_t)P.smax * min(w.m[l], w.n[l])) {
-                        code = 3;                           // a clamp may have reached it: redo in s32
-                    } else if (w.cs[l] != INT32_MIN && w.ub[l] <= w.cs[l]) {   // no path leaving the band scores more
-                        r.flags |= PA_RESULT_BANDED;
-                        r.band_rounds = (uint16_t)L.band_round;
-                        L.out[w.id[l]] = r;
-                        code = 0;
-                    } else {
-                        code = 1;
-                    }
-                    L.band_code[first + l] = code;
-                    if (L.band_ub) L.band_ub[w.id[l]] = w.ub[l];
-                    continue;
-                }
-                if (NL == 2 && MODE != M_LOCAL &&
-                    (int64_t)w.cs[l] <= (int64_t)w.floor_true + (int64_t)P.smax * min(w.m[l], w.n[l])) {
-                    // a clamp may have reached this result: recompute the pair in s32
-                    const uint32_t slot = atomicAdd(L.rerun_count, 1u);
-                    L.rerun_list[slot] = w.id[l];
-                    continue;
-                }
-                L.out[w.id[l]] = r;
-            }
-        }
-        if (MODE == M_BAND && t == 0 && L.dp_cells && w.cells) atomicAdd(L.dp_cells, w.cells);
+        init_work<V, MODE>(L, P, order, first, count, G, R, w);
+        for (int p = 0; p < w.passes; ++p) pass_body<V, R, MODE, GEN, VAR, false>(L, P, w, p, t, G, gmask, snap_store);
+        reduce_group<V, MODE>(w, gmask, G);
+        if (t == 0) emit<V, MODE>(L, P, w, first);
         __syncwarp(gmask);
+    }
+}
+
+// CTA mode for long pairs: the NG = 8 warps of a block are groups of 32 lanes that
+// take the passes of one unit (one pair, two in s16x2 lanes) round robin: pass p
+// runs on warp p % NG, reads the boundary row of pass p - 1 from ring row
+// (p - 1) % NG and writes its own to ring row p % NG, column by column, behind
+// published progress.  Ring row k is reused by pass p + NG only after pass p + 1
+// has read it: pass p + NG reaches column c only after every pass between did.
+template <class V, int R, int MODE, bool GEN, int VAR>
+__global__ void __launch_bounds__(kBlock, 2) dp_kernel_cta(DpLaunch L, DpParams P)
+{
+    static_assert(R % kChunk == 0 && R <= 32, "R must be a multiple of the chunk");
+    constexpr int NL = V::LANES;
+    constexpr int NG = kBlock / 32;
+    constexpr int G = 32;
+    __shared__ uint4 snap_store[MODE == M_LOCAL ? NL * (R / 4) * kBlock : 1];
+    __shared__ int prog[NG];
+    __shared__ uint32_t s_unit;
+    __shared__ int32_t s_cand[NG][2][4];
+    __shared__ int32_t s_lb[MODE == M_LABEL_REV ? NG : 1][8][2];
+    __shared__ unsigned long long s_cells[NG];
+    const int t = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const unsigned gmask = 0xffffffffu;
+    const uint32_t count = *L.count_ptr;
+    const uint32_t *order = L.order + *L.begin_ptr;
+    const uint32_t n_units = (count + NL - 1) / NL;
+    Cell *ring = L.ring + (uint64_t)blockIdx.x * NG * L.ring_stride;
+
+    for (;;) {
+        if (threadIdx.x < NG) prog[threadIdx.x] = -1;
+        if (threadIdx.x == 0) s_unit = atomicAdd(L.unit_counter, 1u);
+        __syncthreads();
+        uint32_t u = s_unit;
+        __syncthreads();
+        if (u >= n_units) break;
+        u = n_units - 1 - u;                         // largest shapes first
+        const uint32_t first = u * NL;
+        GroupWork w;
+        init_work<V, MODE>(L, P, order, first, count, G, R, w);
+        const int32_t span = w.ms + 2;               // progress values of consecutive passes never overlap
+        for (int p = g; p < w.passes; p += NG) {
+            w.bin = ring + (uint64_t)((p + NG - 1) % NG) * L.ring_stride;
+            w.bout = ring + (uint64_t)(p % NG) * L.ring_stride;
+            w.prog_in = &prog[(p + NG - 1) % NG];
+            w.prog_out = &prog[p % NG];
+            w.base_in = (p - 1) * span;
+            w.base_out = p * span;
+            w.seen = INT32_MIN;
+            pass_body<V, R, MODE, GEN, VAR, true>(L, P, w, p, t, G, gmask, snap_store);
+            if (t == G - 1 && p + 1 < w.passes) publish_progress(w.prog_out, w.base_out + w.ms + 1);
+        }
+        reduce_group<V, MODE>(w, gmask, G);
+        if (t == 0) {
+            for (int l = 0; l < 2; ++l) {
+                s_cand[g][l][0] = w.cs[l];
+                s_cand[g][l][1] = w.ci[l];
+                s_cand[g][l][2] = w.cj[l];
+                s_cand[g][l][3] = w.ub[l];
+            }
+            if (MODE == M_LABEL_REV)
+                for (int c = 0; c < 8; ++c) { s_lb[g][c][0] = w.lb_v[c]; s_lb[g][c][1] = w.lb_j[c]; }
+            s_cells[g] = w.cells;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 1; k < NG; ++k) {
+                for (int l = 0; l < 2; ++l) {
+                    const int32_t *c = s_cand[k][l];
+                    if (better(c[0], c[1], c[2], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = c[0]; w.ci[l] = c[1]; w.cj[l] = c[2]; }
+                    w.ub[l] = max(w.ub[l], c[3]);
+                }
+                if (MODE == M_LABEL_REV)
+                    for (int c = 0; c < 8; ++c) {
+                        const int32_t ov = s_lb[k][c][0], oj = s_lb[k][c][1];
+                        if (ov > w.lb_v[c] || (ov == w.lb_v[c] && oj < w.lb_j[c])) { w.lb_v[c] = ov; w.lb_j[c] = oj; }
+                    }
+                w.cells += s_cells[k];
+            }
+            emit<V, MODE>(L, P, w, first);
+        }
+        __syncthreads();
     }
 }
 

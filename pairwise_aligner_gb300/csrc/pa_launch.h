@@ -12,4 +12,10 @@ int dp_occupancy(int variant, bool lanes16, bool gen, int mode);
 void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStream_t stream, const DpLaunch &L,
                const DpParams &P);
 
+// CTA mode (long pairs): whole blocks per pair; L.ring must hold grid * 8 rows of
+// L.ring_stride cells.
+int dp_cta_occupancy(bool lanes16, bool gen, int mode);
+void dp_cta_launch(bool lanes16, bool gen, int mode, int grid, cudaStream_t stream, const DpLaunch &L,
+                   const DpParams &P);
+
 }  // namespace pa

@@ -14,14 +14,17 @@ struct ClassCfg {
     int32_t s16_params;      // gap scores small enough for s16 lanes
     int32_t force32;         // width hint 32
     int32_t local;
-    int32_t rows[3];         // rows per pass (G*R) of each DP class
-    int32_t gcnt[3];         // G of each class (for the last-pass chunk count)
-    int32_t rpt[3];          // R of each class
+    int32_t rows[kClasses];  // rows per pass (G*R) of each DP class
+    int32_t gcnt[kClasses];  // G of each class (for the last-pass chunk count)
+    int32_t rpt[kClasses];   // R of each class
+    int64_t long_cells;      // pairs with m*n at least this (and m <= long_max_m) go to CTA mode
+    int32_t long_max_m;      // the longest sequence1 the CTA ring rows hold
+    int32_t pad;
 };
 
 struct PrepStats {
     unsigned long long cells;
-    unsigned long long n_class[4];
+    unsigned long long n_class[8];
     unsigned long long overflow;    // pairs whose int32 bound fails
 };
 
@@ -79,7 +82,7 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
     const uint32_t match4 = (uint8_t)P.match * 0x01010101u;
     const uint32_t mis4 = (uint8_t)P.mismatch * 0x01010101u;
     // statistics are summed per lane 0 and per block, then added once per block
-    unsigned long long my_cells = 0, my_class[4] = {0, 0, 0, 0}, my_overflow = 0;
+    unsigned long long my_cells = 0, my_class[8] = {0, 0, 0, 0, 0, 0, 0, 0}, my_overflow = 0;
     for (uint64_t p = warp; p < n_pairs; p += nwarps) {
         const uint64_t q0 = off1[p], t0 = off2[p];
         const int64_t m = (int64_t)(off1[p + 1] - q0), n = (int64_t)(off2[p + 1] - t0);
@@ -98,7 +101,8 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
         else if (!C.fast_scores || !dna) klass = K_GEN;
         else if (!C.force32 && C.s16_params && (int64_t)P.smax * min(m, n) <= 30000) klass = K_S16;
         else klass = K_S32;
-        if (klass == K_S16 || klass == K_S32) {
+        if (klass != K_NONE && m * n >= C.long_cells && m <= C.long_max_m && n <= (1 << 20)) klass += kLongOffset;
+        if (klass == K_S16 || klass == K_S32 || klass == K_S16L || klass == K_S32L) {
             uint32_t *qt = qtab + q0 + p;
             for (int64_t i = 4 * lane; i <= m; i += 128) {
                 const uint8_t *a = seq1 + q0 + i;
@@ -134,21 +138,21 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
             ++my_class[klass];
         }
     }
-    __shared__ unsigned long long sh[6];
-    if (threadIdx.x < 6) sh[threadIdx.x] = 0;
+    __shared__ unsigned long long sh[10];
+    if (threadIdx.x < 10) sh[threadIdx.x] = 0;
     __syncthreads();
     if (lane == 0) {
         if (my_cells) atomicAdd(&sh[0], my_cells);
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < 8; ++k)
             if (my_class[k]) atomicAdd(&sh[1 + k], my_class[k]);
-        if (my_overflow) atomicAdd(&sh[5], my_overflow);
+        if (my_overflow) atomicAdd(&sh[9], my_overflow);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         if (sh[0]) atomicAdd(&st->cells, sh[0]);
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < 8; ++k)
             if (sh[1 + k]) atomicAdd(&st->n_class[k], sh[1 + k]);
-        if (sh[5]) atomicAdd(&st->overflow, sh[5]);
+        if (sh[9]) atomicAdd(&st->overflow, sh[9]);
     }
 }
 
@@ -216,8 +220,8 @@ __global__ void k_scatter(const uint32_t *__restrict__ keys, uint64_t n_pairs, u
 {
     const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (p == 0) {
-        // class sizes from the class begins (ranges[4] = number of non-trivial pairs)
-        for (int c = 0; c < 3; ++c) counts[c] = ranges[c + 1] - ranges[c];
+        // class sizes from the class begins (class 7 holds no keys: ranges[7] is the end)
+        for (int c = 0; c < kClasses; ++c) counts[c] = ranges[c + 1] - ranges[c];
     }
     if (p >= n_pairs) return;
     const uint32_t key = keys[p];

@@ -120,6 +120,8 @@ __global__ void __launch_bounds__(pa::kBlock, 2) dp_kernel_static(pa::DpLaunch L
         w.rows_full = G * R;
         w.passes = (w.nh + w.rows_full - 1) / w.rows_full;
         w.buf = L.boundary + (L.off1[first] + first);
+        w.bin = w.bout = w.buf;
+        w.seen = INT32_MIN;
         w.Kt = 0;
         w.clampt = MODE == M_LOCAL ? 0 : INT32_MIN;
         w.floor_true = INT32_MIN;

@@ -261,6 +261,16 @@ def subset(d: dict, idx: np.ndarray) -> dict:
     return out
 
 
+def concat(ds: list[dict]) -> dict:
+    """The pairs of several workloads of one scoring, in order."""
+    out = {k: v for k, v in ds[0].items() if k not in ("seq1", "off1", "seq2", "off2", "related", "stratum")}
+    for s, o in (("seq1", "off1"), ("seq2", "off2")):
+        out[s] = np.concatenate([d[s] for d in ds])
+        lens = np.concatenate([np.diff(d[o].astype(np.int64)) for d in ds])
+        out[o] = _offsets(lens)
+    return out
+
+
 def cells(d: dict) -> int:
     m = np.diff(d["off1"].astype(np.int64))
     n = np.diff(d["off2"].astype(np.int64))
