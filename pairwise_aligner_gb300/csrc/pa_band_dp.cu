@@ -119,9 +119,12 @@ __global__ void k_band_windows(const uint64_t *__restrict__ off1, const uint64_t
 }
 
 // Network outputs (16 floats per pair, 9 used) -> band: checkpoint diagonals
-// out[c] * (m + n) / 4 and, from the predicted cost c2 = 2^(16 out[8]) - 1 (the
-// score deficit smax (m + n) - 2 S), the starting half-width that a path
-// leaving the band must pay for in gaps: (c2 / 2 - 2 |open|) / (2 |ext| + smax).
+// out[c] * (m + n) / 4 and, from the predicted deficit c2 = 2^(16 out[8]) - 1
+// (= smax (m + n) - 2 S), the starting half-width.  A path that leaves the band
+// by d diagonals and comes back pays two gap opens and at least d extensions
+// while the diagonal steps it gives up could gain at most smax each; the band
+// proves itself once that cost exceeds the deficit D = c2 / 2 of the rest of the
+// alignment: d >= (D - 2 |open|) / (|ext| + smax).
 __global__ void k_band_decode(const float *__restrict__ out, const uint64_t *__restrict__ off1,
                               const uint64_t *__restrict__ off2, uint64_t n_pairs, DpParams P, float margin,
                               int32_t w_min, BandSpec *__restrict__ spec)
@@ -134,7 +137,7 @@ __global__ void k_band_decode(const float *__restrict__ out, const uint64_t *__r
     const float scale = (float)(m + n) * 0.25f;
     for (int c = 0; c < 8; ++c) B.diag[c] = __float2int_rn(o[c] * scale);
     const float c2 = exp2f(fminf(o[8], 1.5f) * 16.f) - 1.f;
-    const float per = (float)(2 * (-P.gap_ext) + P.smax);
+    const float per = (float)(-P.gap_ext + P.smax);
     float ws = (0.5f * c2 + 2.f * (float)P.gap_open) / (per > 0.f ? per : 1.f);
     ws = margin * fmaxf(ws, 0.f) + (float)w_min;
     const float cap = (float)max(m, n) + 1.f;

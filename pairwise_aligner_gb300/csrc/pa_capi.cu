@@ -138,9 +138,11 @@ pa_status check_config(pa_ctx *c, const pa_config *cfg, DpParams &P, ClassCfg &C
     P.last_row_free = !local && cfg->last_row_free;
     P.smax = std::max(0, std::max(cfg->match, cfg->mismatch));
     P.spad = std::min(0, std::min(cfg->match, cfg->mismatch));
+    P.shift = local ? 0 : P.smax;
     P.floor16 = -32768 + 1280;
     std::memset(&C, 0, sizeof(C));
-    C.fast_scores = cfg->match >= -127 && cfg->match <= 127 && cfg->mismatch >= -127 && cfg->mismatch <= 0;
+    C.fast_scores = cfg->match >= -127 && cfg->match <= 127 && cfg->mismatch >= -127 && cfg->mismatch <= 0 &&
+                    cfg->match - P.shift >= -128 && cfg->mismatch - P.shift >= -128;   // byte tables of shifted scores
     C.s16_params = (int64_t)cfg->gap_open + cfg->gap_extension >= -1000 && cfg->gap_extension >= -1000;
     C.force32 = cfg->width_hint == 32;
     C.local = local;

@@ -16,6 +16,7 @@ struct DpParams {
     int32_t floor16;      // lower clamp of s16 global lanes
     int32_t smax;         // max(match, mismatch, 0): best gain of one diagonal step
     int32_t spad;         // score of a padded cell, <= 0 and <= every real score
+    int32_t shift;        // global modes store H(i, j) - shift * i with shift = smax (local: 0)
 };
 
 // Work classes produced by the classifier; the class is the top field of the bucket key.

@@ -219,12 +219,17 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
 {
     constexpr int NL = V::LANES;
     const int32_t j0 = p * w.rows_full + t * RA;   // rows j0+1 .. j0+RA (1-based)
+    // vertical steps (along sequence2) cost the gap scores; horizontal steps (to the next
+    // column) also subtract the column shift of global modes (P.shift = smax, local 0)
     const uint32_t GOEA = V::cabs(P.gap_open + P.gap_ext);
     const uint32_t EXTA = V::cabs(P.gap_ext);
+    const uint32_t GOEH = V::cabs(P.gap_open + P.gap_ext - P.shift);
+    const uint32_t EXTH = V::cabs(P.gap_ext - P.shift);
     const uint32_t CLAMP = w.CLAMP;
     const uint32_t CLAMPG = V::LANES == 2 ? V::subc(CLAMP, GOEA) : (uint32_t)max((int)CLAMP, INT32_MIN + 65536) - GOEA;
 
     constexpr bool BAND = MODE == M_BAND;
+    constexpr bool SHIFTED = MODE != M_LOCAL;       // H is stored as H - shift * column
     const int32_t ibase = BAND ? w.ibase : 0;      // the pass sweeps columns ibase+1 .. iend
     const int32_t iend = BAND ? w.iend : w.ms;
     const int32_t msw = iend - ibase;
@@ -243,13 +248,13 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
         }
         Sel[k] = GEN ? (uint32_t)c[0] : V::selector(c[0], c[1]);
         H[k] = left_out ? NEGV : stored<V>(w, border(P, P.first_row_free, (int64_t)j + 1));
-        Fr[k] = V::subc(H[k], GOEA);
+        Fr[k] = V::subc(H[k], GOEH);
     }
     uint32_t prevH = left_out ? (t == 0 ? w.diag0 : NEGV) : stored<V>(w, border(P, P.first_row_free, j0));
     uint32_t topH = prevH;                              // thread 0, pass 0: H(i-1, 0)
     uint32_t top_last = NEGV;                           // band: thread 0's top input at column iend
-    const uint32_t step1 = P.first_column_free ? 0u : V::cabs(P.gap_open + P.gap_ext);
-    const uint32_t stepn = P.first_column_free ? 0u : EXTA;
+    const uint32_t step1 = V::cabs((P.first_column_free ? 0 : P.gap_open + P.gap_ext) - P.shift);
+    const uint32_t stepn = V::cabs((P.first_column_free ? 0 : P.gap_ext) - P.shift);
     uint32_t outH = 0, outE = 0, best = w.K;
     int32_t bi[2] = {0, 0};
     int32_t own_k[2], own_t[2];
@@ -330,7 +335,8 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             uint32_t sc;
             if (GEN) {
                 const uint32_t x = Sel[k];
-                sc = (x == ta) ? (uint32_t)P.match : (((x | ta) >> 8) ? (uint32_t)P.spad : (uint32_t)P.mismatch);
+                sc = (x == ta) ? (uint32_t)(P.match - P.shift)
+                               : (((x | ta) >> 8) ? (uint32_t)(P.spad - P.shift) : (uint32_t)(P.mismatch - P.shift));
             } else {
                 sc = prmt(ta, tb, Sel[k]);
             }
@@ -341,20 +347,20 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
                 // vertical gap is dominated, so the serial chain is one IADD and one VIMAX3
                 const uint32_t h = V::hmax(tt, Ed, CLAMP);
                 H[k] = h;
-                Fr[k] = V::max2(V::subc(Fr[k], EXTA), V::subc(h, GOEA));
+                Fr[k] = V::max2(V::subc(Fr[k], EXTH), V::subc(h, GOEH));
                 Ed = V::max3(V::subc(Ed, EXTA), V::subc(tt, GOEA), CLAMPG);
             } else if ((VAR & 1) == 0) {
                 const uint32_t h = V::hmax(tt, Ed, CLAMP);
                 H[k] = h;
                 const uint32_t hoe = V::subc(h, GOEA);
-                Fr[k] = V::max2(V::subc(Fr[k], EXTA), hoe);
+                Fr[k] = V::max2(V::subc(Fr[k], EXTH), SHIFTED ? V::subc(h, GOEH) : hoe);
                 Ed = V::max2(V::subc(Ed, EXTA), hoe);
             } else {
                 // vgap' = max(vgap + ext, max(t, clamp) + open + ext): H leaves the serial chain
                 const uint32_t x = V::max2(tt, CLAMP);
                 const uint32_t h = V::max2(x, Ed);
                 H[k] = h;
-                Fr[k] = V::max2(V::subc(Fr[k], EXTA), V::subc(h, GOEA));
+                Fr[k] = V::max2(V::subc(Fr[k], EXTH), V::subc(h, GOEH));
                 Ed = V::max2(V::subc(Ed, EXTA), V::subc(x, GOEA));
             }
         }
@@ -378,13 +384,13 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
                     if (t == 0 && p == 0) dc[0] = border(P, P.first_column_free, i);
 #pragma unroll
                     for (int k = 0; k < RA; ++k)
-                        if (j0 + k + 1 <= n0) dc[j0 + k + 1] = V::get(H[k], 0) - w.Kt;
+                        if (j0 + k + 1 <= n0) dc[j0 + k + 1] = V::get(H[k], 0) - w.Kt + P.shift * i;
                 } else {
 #pragma unroll
                     for (int k = 0; k < RA; ++k) {
                         const int32_t jf = n0 - (j0 + k + 1);            // forward row
                         if (jf >= 0) {
-                            const int32_t v = dc[jf] + V::get(H[k], 0) - w.Kt;
+                            const int32_t v = dc[jf] + V::get(H[k], 0) - w.Kt + P.shift * i;
                             if (v > w.lb_v[c] || (v == w.lb_v[c] && jf < w.lb_j[c])) { w.lb_v[c] = v; w.lb_j[c] = jf; }
                         }
                     }
@@ -417,7 +423,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
 #pragma unroll
                     for (int k = 1; k < RA; ++k)
                         if (own_k[l] == k) v = H[k];
-                    const int32_t xs = V::get(v, l) - w.Kt;
+                    const int32_t xs = V::get(v, l) - w.Kt + P.shift * i;
                     if (better(xs, i, w.n[l], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = xs; w.ci[l] = i; w.cj[l] = w.n[l]; }
                 }
                 if (i == w.m[l]) {
@@ -426,7 +432,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
                         for (int k = 0; k < RA; ++k) {
                             const int32_t j = j0 + k + 1;
                             if (j <= w.n[l]) {
-                                const int32_t xs = V::get(H[k], l) - w.Kt;
+                                const int32_t xs = V::get(H[k], l) - w.Kt + P.shift * i;
                                 if (better(xs, i, j, w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = xs; w.ci[l] = i; w.cj[l] = j; }
                             }
                         }
@@ -435,7 +441,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
 #pragma unroll
                         for (int k = 1; k < RA; ++k)
                             if (own_k[l] == k) v = H[k];
-                        const int32_t xs = V::get(v, l) - w.Kt;
+                        const int32_t xs = V::get(v, l) - w.Kt + P.shift * i;
                         if (better(xs, i, w.n[l], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = xs; w.ci[l] = i; w.cj[l] = w.n[l]; }
                     }
                 }
@@ -468,8 +474,8 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             for (int k = 0; k < RA; ++k) {
                 const int32_t j = j0 + k + 1;
                 if (j > w.n[l]) continue;
-                const int32_t gv = V::get(Fr[k], l) - w.Kt;
-                const int32_t dv = V::get(k == 0 ? hup0 : H[k - 1], l) - w.Kt + P.smax;
+                const int32_t gv = V::get(Fr[k], l) - w.Kt + P.shift * (iend + 1);
+                const int32_t dv = V::get(k == 0 ? hup0 : H[k - 1], l) - w.Kt + P.shift * iend + P.smax;
                 w.ub[l] = max(w.ub[l], exit_bound(P, gv, dv, iend + 1, j, w.m[l], w.n[l]));
             }
         }
@@ -533,8 +539,8 @@ __device__ __forceinline__ void init_work(const DpLaunch &L, const DpParams &P, 
             w.clampt = 2048;
             w.floor_true = 0;
         } else {
-            const int32_t ub = P.smax * max(min(w.m[0], w.n[0]), min(w.m[1], w.n[1]));
-            w.Kt = 32767 - 512 - ub;
+            // stored H - smax * column never exceeds 0 (no step gains more than the shift)
+            w.Kt = 32767 - 512;
             w.clampt = 2048;
             w.floor_true = 2048 - w.Kt;
         }
@@ -626,9 +632,10 @@ __device__ __forceinline__ void pass_body(const DpLaunch &L, const DpParams &P, 
                 const int32_t last = min(min(bcur.y, bnext.x - 1), ml);
                 for (int32_t i = bcur.x + t; i <= last; i += G) {
                     const Cell c = w.bout[i];
-                    w.ub[l] = max(w.ub[l], exit_bound(P, V::get(c.e, l) - w.Kt, kNeg32, i, jhi + 1, ml, nl));
+                    const int32_t cv = P.shift * i - w.Kt;
+                    w.ub[l] = max(w.ub[l], exit_bound(P, V::get(c.e, l) + cv, kNeg32, i, jhi + 1, ml, nl));
                     if (i + 1 < bnext.x)
-                        w.ub[l] = max(w.ub[l], exit_bound(P, kNeg32, V::get(c.h, l) - w.Kt + P.smax, i + 1,
+                        w.ub[l] = max(w.ub[l], exit_bound(P, kNeg32, V::get(c.h, l) + cv + P.smax, i + 1,
                                                           jhi + 1, ml, nl));
                 }
             }
@@ -695,7 +702,7 @@ __device__ __forceinline__ void emit(const DpLaunch &L, const DpParams &P, Group
         if (MODE == M_LOCAL && w.cs[l] <= 0) { r.end1 = 0; r.end2 = 0; }
         if (MODE == M_BAND) {
             uint8_t code;
-            if (NL == 2 && (int64_t)w.cs[l] <= (int64_t)w.floor_true + (int64_t)P.smax * min(w.m[l], w.n[l])) {
+            if (NL == 2 && (int64_t)w.cs[l] - (int64_t)P.shift * w.ci[l] <= (int64_t)w.floor_true) {
                 code = 3;                           // a clamp may have reached it: redo in s32
             } else if (w.cs[l] != INT32_MIN && w.ub[l] <= w.cs[l]) {   // no path leaving the band scores more
                 r.flags |= PA_RESULT_BANDED;
@@ -709,9 +716,9 @@ __device__ __forceinline__ void emit(const DpLaunch &L, const DpParams &P, Group
             if (L.band_ub) L.band_ub[w.id[l]] = w.ub[l];
             continue;
         }
-        if (NL == 2 && MODE != M_LOCAL &&
-            (int64_t)w.cs[l] <= (int64_t)w.floor_true + (int64_t)P.smax * min(w.m[l], w.n[l])) {
-            // a clamp may have reached this result: recompute the pair in s32
+        if (NL == 2 && MODE != M_LOCAL && (int64_t)w.cs[l] - (int64_t)P.shift * w.ci[l] <= (int64_t)w.floor_true) {
+            // every step adds at most 0 to H - shift * column, so a clamped cell stays at or
+            // below the floor: a result above it never met a clamp.  Otherwise recompute in s32
             const uint32_t slot = atomicAdd(L.rerun_count, 1u);
             L.rerun_list[slot] = w.id[l];
             continue;

@@ -79,8 +79,8 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
     const int lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const uint32_t match4 = (uint8_t)P.match * 0x01010101u;
-    const uint32_t mis4 = (uint8_t)P.mismatch * 0x01010101u;
+    const uint32_t match4 = (uint8_t)(P.match - P.shift) * 0x01010101u;     // scores of H - shift * column
+    const uint32_t mis4 = (uint8_t)(P.mismatch - P.shift) * 0x01010101u;
     // statistics are summed per lane 0 and per block, then added once per block
     unsigned long long my_cells = 0, my_class[8] = {0, 0, 0, 0, 0, 0, 0, 0}, my_overflow = 0;
     for (uint64_t p = warp; p < n_pairs; p += nwarps) {
@@ -99,7 +99,10 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
         uint32_t klass;
         if (m == 0 || n == 0) klass = K_NONE;
         else if (!C.fast_scores || !dna) klass = K_GEN;
-        else if (!C.force32 && C.s16_params && (int64_t)P.smax * min(m, n) <= 30000) klass = K_S16;
+        // s16 lanes: local scores stay in [0, smax min(m, n)]; global lanes hold H - smax * column,
+        // which is at most 0, and a result is exact when that value of its end cell is above
+        // the clamp floor (checked after the DP), so any length may try s16 first
+        else if (!C.force32 && C.s16_params && (!C.local || (int64_t)P.smax * min(m, n) <= 30000)) klass = K_S16;
         else klass = K_S32;
         if (klass != K_NONE && m * n >= C.long_cells && m <= C.long_max_m && n <= (1 << 20)) klass += kLongOffset;
         if (klass == K_S16 || klass == K_S32 || klass == K_S16L || klass == K_S32L) {
@@ -115,7 +118,7 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
             const int64_t a = P.match < 0 ? -(int64_t)P.match : P.match;
             const int64_t b = P.mismatch < 0 ? -(int64_t)P.mismatch : P.mismatch;
             const int64_t o = -(int64_t)P.gap_open, e = -(int64_t)P.gap_ext;
-            const int64_t bound = (a + b) * min(m, n) + (o + e) * (m + n + 2) + 2 * o;
+            const int64_t bound = (a + b) * min(m, n) + (o + e) * (m + n + 2) + 2 * o + (int64_t)P.shift * (m + n);
             if (bound >= (1ll << 30)) ++my_overflow;
             uint32_t key;
             if (klass == K_NONE) {

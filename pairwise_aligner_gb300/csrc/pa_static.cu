@@ -13,6 +13,7 @@
 // The kernel is a variant of dp_kernel<L32, byte-compare>: pairs are taken in
 // input order (no bucketing, so no keys, histogram or score tables are needed),
 // one pair per group of 8 lanes, s32 arithmetic, raw byte equality.
+#include <cstring>
 #include <mutex>
 
 #include "pa_dp.cuh"
@@ -230,8 +231,10 @@ extern "C" pa_status pa_align_batch_device_static(const pa_config *config, const
     P.spad = config->match < config->mismatch ? config->match : config->mismatch;
     if (P.spad > 0) P.spad = 0;
     P.floor16 = 0;
+    P.shift = 0;                 // s32 lanes hold H itself
 
     DpLaunch L;
+    std::memset(&L, 0, sizeof(L));
     L.seq1 = d_seq1; L.off1 = d_off1; L.seq2 = d_seq2; L.off2 = d_off2;
     L.qtab = nullptr; L.order = nullptr; L.begin_ptr = nullptr; L.count_ptr = nullptr;
     L.unit_counter = slot->counters;

@@ -225,7 +225,7 @@ def _true_bands(oracle, d, al, margin=1.5, w_min=16):
     n = np.diff(d["off2"].astype(np.int64))
     smax = max(d["match"], 0)
     c2 = smax * (m + n) - 2 * sc
-    per = 2 * (-d["gap_extension"]) + smax
+    per = -d["gap_extension"] + smax
     ws = np.maximum((c2 / 2 + 2 * d["gap_open"]) / per, 0) * margin + w_min
     b = np.zeros((len(m), 10), np.int32)
     b[:, :8] = lab
