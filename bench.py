@@ -22,6 +22,11 @@ One step = one call of the hot path over the whole batch:
 build when present, else the oracle's SIMD port) on the host cores.
 N > 1 GPUs (torchrun): independent replicas, one full batch per rank, no
 collective on the data path; value = all ranks' cells / max time.
+
+--workload config1..config5 measures the other seeded workloads the same way
+(config 3: 8,192 long reads; config 5: the 1,048,576-pair mixed stream), and
+--band 1 / 2 runs global workloads in band mode (learned band with the shipped
+predictor weights / straight band); scores are the same as --band 0.
 """
 from __future__ import annotations
 
@@ -38,7 +43,9 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 METRIC = "GCUPS (m*n cells/s), affine-gap local score DP + end coordinates, bit-exact"
+METRIC_GLOBAL = "GCUPS (m*n cells/s), affine-gap global score DP, bit-exact"
 WORKLOAD = "config2_local_262144_pairs_64-512bp_+1/-4/-6/-1"
+BAND_MODEL = os.path.join(REPO, "pairwise_aligner_gb300", "data", "band_model.npz")
 # DRAM bytes per cell of the s16x2 local DP kernel, from the ncu capture summarised in
 # profiles/dp_kernel_s16x2_local_config2.md (dram__bytes_read.sum + dram__bytes_write.sum
 # of a 32,768-pair launch divided by its 2.71e9 cells; traffic grows with the cells).
@@ -105,10 +112,34 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def load_workload(pairs: int | None):
+def load_workload(pairs: int | None, workload: str = "config2"):
+    """The seeded workload; with PA_WORKLOAD_CACHE set, generated once per directory."""
+    import numpy as np
     from pairwise_aligner_gb300 import workloads as W
-    d = W.config2() if not pairs else W.config2(n_pairs=pairs)
+    cache = os.environ.get("PA_WORKLOAD_CACHE")
+    path = os.path.join(cache, f"{workload}_{pairs or 0}.npz") if cache else None
+    if path and os.path.exists(path):
+        z = np.load(path, allow_pickle=False)
+        d = {k: z[k] for k in z.files}
+        for k in ("local",):
+            d[k] = bool(d[k])
+        for k in ("match", "mismatch", "gap_open", "gap_extension", "config"):
+            d[k] = int(d[k])
+        d["name"] = str(d["name"])
+        return d, W.cells(d)
+    gen = W.GENERATORS[int(workload[-1])]
+    d = gen() if not pairs else gen(n_pairs=pairs)
+    if path:
+        os.makedirs(cache, exist_ok=True)
+        np.savez(path + ".tmp.npz", **{k: np.asarray(v) for k, v in d.items()})
+        os.replace(path + ".tmp.npz", path)
     return d, W.cells(d)
+
+
+def workload_name(d: dict, workload: str, n: int) -> str:
+    if workload == "config2":
+        return WORKLOAD
+    return f"{d.get('name', workload)}_{n}_pairs_{d['match']:+d}/{d['mismatch']:+d}/{d['gap_open']:+d}/{d['gap_extension']:+d}"
 
 
 def cpu_sample_rate(d, budget_s: float, threads: int):
@@ -136,7 +167,7 @@ def reference_arm(args):
         return 0
     from oracle import oracle as O
     from pairwise_aligner_gb300 import workloads as W
-    d, _ = load_workload(args.pairs)
+    d, _ = load_workload(args.pairs, args.workload)
     threads = os.cpu_count() or 1
     kind, label = "port", "oracle inter-sequence int16 SIMD port (oracle/pa_oracle.c), pthreads"
     ref_lib = os.path.join(REPO, "oracle", "_ref", "libpa_ref.so")
@@ -157,10 +188,11 @@ def reference_arm(args):
     cells = W.cells(sub)
     value = cells * len(times) / sum(times) / 1e9
     sample = f"first {n} of {len(d['off1']) - 1} pairs ({cells:.3g} cells) per step; {label}"
-    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GCUPS", "n_gpus": args.gpus,
+    line = {"impl": "reference", "metric": METRIC if d["local"] else METRIC_GLOBAL, "value": round(value, 3), "unit": "GCUPS", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16 lanes",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "pairs_per_step": n},
+            "data": "synthetic", "config": {"workload": workload_name(d, args.workload, len(d["off1"]) - 1),
+                                            "pairs_per_step": n},
             "cpu_baseline": {"value": round(value, 3), "unit": "GCUPS", "cores": threads, "kind": kind,
                              "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -182,12 +214,20 @@ def our_arm(args):
     B.build()
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    d, cells = load_workload(args.pairs)
+    d, cells = load_workload(args.pairs, args.workload)
     n = len(d["off1"]) - 1
+    free = bool(d["local"])
+    if args.band and d["local"]:
+        raise SystemExit("--band applies to the global workloads (config1, config3, config4, config5)")
     conf = dict(local=d["local"], match=d["match"], mismatch=d["mismatch"], gap_open=d["gap_open"],
-                gap_extension=d["gap_extension"], first_column_free=True, first_row_free=True,
-                last_column_free=True, last_row_free=True, width_hint=0, band_mode=0)
+                gap_extension=d["gap_extension"], first_column_free=free, first_row_free=free,
+                last_column_free=free, last_row_free=free, width_hint=0, band_mode=args.band)
     ctx = pa.Context(local_rank, group_threads=args.group_threads, kernel_variant=args.variant)
+    if args.band == 1:
+        from pairwise_aligner_gb300 import band as BD
+        model = BD.BandModel(device=dev)
+        model.load(BAND_MODEL)
+        model.to_context(ctx)
     al = Aligner(conf, device=local_rank, context=ctx)
     peak = ctx.roofline()
 
@@ -209,19 +249,36 @@ def our_arm(args):
     torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
+    # inputs smaller than L2 (the small workloads): time every step alone, after an L2 flush
+    small = int(d["off1"][-1] + d["off2"][-1]) * 3 + 16 * n < 129e6
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev) if small else None
     with ClockSampler(local_rank) as clk:
         time.sleep(0.3)
-        e0.record(stream)
-        for _ in range(args.steps):
-            al.compute_device(s1, o1, s2, o2, out, stream=stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
+        if small:
+            total = 0.0
+            for _ in range(args.steps):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                al.compute_device(s1, o1, s2, o2, out, stream=stream)
+                b.record(stream)
+                b.synchronize()
+                total += a.elapsed_time(b)
+            step_ms = total / args.steps
+        else:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                al.compute_device(s1, o1, s2, o2, out, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            step_ms = e0.elapsed_time(e1) / args.steps
         time.sleep(0.3)
     barrier()
     torch.cuda.synchronize()
-    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
+    ms = max_over_ranks(step_ms, world)
     value = replica_throughput(cells, ms, world)
 
     # DP kernels alone (events inside the library, same stream), one call at a time
@@ -252,18 +309,21 @@ def our_arm(args):
     peak_gcups = peak["s16x2_cells_per_s"] / 1e9
     alg_bytes = int(d["off1"][-1] + d["off2"][-1]) + 16 * n          # inputs read + results written
     line = {
-        "metric": METRIC, "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
+        "metric": METRIC if d["local"] else METRIC_GLOBAL, "value": round(value, 2), "unit": "GCUPS",
+        "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int16x2 lanes (int32 where a pair needs it)", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "pairs": n, "cells": cells, "group_threads": ctx_G(args),
-                   "l2": "inputs (~150 MB bytes + ~300 MB score tables) larger than the 129 MB L2; no flush",
+        "config": {"workload": workload_name(d, args.workload, n), "pairs": n, "cells": cells,
+                   "group_threads": ctx_G(args), "band_mode": args.band,
+                   "l2": ("inputs (bytes + 4-byte score tables) larger than the 129 MB L2; no flush" if not small
+                          else "inputs smaller than L2: a 256 MB buffer is written before every timed step"),
                    "pairs_s16": st["pairs_s16"], "pairs_s32": st["pairs_s32"], "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(replica_throughput(cells, e2e_s * 1e3, world), 2), "unit": "GCUPS",
                 "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "int_dpx", "achieved": round(achieved, 1), "peak": round(peak_gcups, 1),
                      "unit": "GCUPS", "frac": round(achieved / peak_gcups, 4),
-                     "traffic": int(DRAM_BYTES_PER_CELL * cells),
+                     "traffic": int(DRAM_BYTES_PER_CELL * cells) if args.workload == "config2" else None,
                      "peak_source": "pa_measure_roofline: whole-chip s16x2 cell-update instruction mix, measured live",
                      "kernel": "dp_kernel<L16> (all DP kernels of one call)", "kernel_ms": round(dp_ms, 4),
                      "hbm": {"achieved": round(alg_bytes / (dp_ms * 1e-3) / 1e9, 1),
@@ -272,6 +332,8 @@ def our_arm(args):
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
     }
+    if args.band:
+        line["band"] = {k: st[k] for k in ("pairs_banded", "pairs_full_dp", "band_cells", "band_rounds")}
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rate, npairs, dt = cpu_sample_rate(d, args.cpu_seconds, threads)
@@ -323,6 +385,9 @@ def main():
     ap.add_argument("--variant", type=int, default=-1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", choices=["config1", "config2", "config3", "config4", "config5"], default="config2")
+    ap.add_argument("--band", type=int, choices=[0, 1, 2], default=0,
+                    help="band mode for global workloads: 1 learned (shipped weights), 2 straight")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
