@@ -219,6 +219,11 @@ pa_status pa_mlp_to_bf16(const float *src, int rows, int cols, int ld_dst, void 
  * lanes; default 2^22.  1 sends every pair there, UINT64_MAX none. */
 pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells);
 
+/* Of those, pairs with at least `cells` cells and `min_rows` rows of sequence2 are
+ * computed by clusters of 4 thread blocks (co-scheduled; their 32 warps pipeline the
+ * pair's passes); defaults 2^28 and 8192. */
+pa_status pa_set_cluster_threshold(pa_ctx *ctx, uint64_t cells, uint32_t min_rows);
+
 /* Band mode (no counterpart in the reference, which has no banded mode).
  * A pair's band: the centre line through (0, 0), the checkpoints
  * (i_c, i_c + diag[c]) with i_c = (c + 1) * m / 9, c = 0..7, and (m, n),

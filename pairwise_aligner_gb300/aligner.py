@@ -65,6 +65,10 @@ class Context:
         """Pairs with at least `cells` m*n cells run on whole thread blocks (1: all pairs)."""
         _lib.check(self.lib.pa_set_cta_threshold(self.ptr, int(cells)), self.ptr)
 
+    def set_cluster_threshold(self, cells: int, min_rows: int = 8192):
+        """Of the block-mode pairs, those with at least `cells` cells and `min_rows` rows run on clusters."""
+        _lib.check(self.lib.pa_set_cluster_threshold(self.ptr, int(cells), int(min_rows)), self.ptr)
+
     # -- band mode ----------------------------------------------------------------
     def band_options(self) -> dict:
         o = _lib.PaBandOptions()

@@ -54,6 +54,8 @@ struct pa_ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     cudaEvent_t ev_dp0 = nullptr, ev_dp1 = nullptr;   // bracket the DP kernels of the last call
+    cudaStream_t side = nullptr;                      // cluster-mode kernels run beside the others
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     pa_options opt{};
     std::string err;
     // device work buffers (grow only)
@@ -62,6 +64,8 @@ struct pa_ctx {
     int32_t ring_m = 0;           // longest sequence1 the ring rows hold (0: no CTA mode yet)
     int ring_grid = 0;            // blocks of every CTA-mode launch
     int64_t long_cells = 1ll << 22;   // pairs with at least this many cells use CTA mode
+    int64_t huge_cells = 1ll << 28;   // ... and with this many (and n >= huge_min_n) cluster mode
+    int32_t huge_min_n = 8192;
     int64_t want_ring_m = 0;          // the next call's longest CTA-mode sequence1 (host: exact)
     DevBuf in_seq1, in_off1, in_seq2, in_off2, in_out;   // staging for the host-buffer entry points
     int G[3] = {kDefaultG, kDefaultG, kDefaultG};
@@ -74,12 +78,18 @@ struct pa_ctx {
     // band mode
     pa_band_options band_opt{1.25f, 16, 64, 0.5f, 6, {0, 0, 0}};
     DevBuf band_spec, band_win, band_code, band_bsum, band_ctr, band_in;
-    DevBuf band_list[16];
+    DevBuf band_list[20];
     DevBuf mlp_w[6], mlp_feat, mlp_x, mlp_h1, mlp_h2, mlp_out;
     bool has_model = false;
 };
 
 namespace {
+
+// The ring rows of cluster-mode launches (CTA-mode launches use the first region).
+Cell *cluster_ring(pa_ctx *c)
+{
+    return (Cell *)c->ring.p + (size_t)c->ring_grid * 8 * ((size_t)c->ring_m + 2);
+}
 
 pa_status fail(pa_ctx *c, pa_status s, const std::string &msg)
 {
@@ -153,6 +163,8 @@ pa_status check_config(pa_ctx *c, const pa_config *cfg, DpParams &P, ClassCfg &C
         C.rows[k] = C.gcnt[k] * kR;
     }
     C.long_cells = c->long_cells;
+    C.huge_cells = c->huge_cells;
+    C.huge_min_n = c->huge_min_n;
     C.long_max_m = c->ring.p ? c->ring_m : 0;
     return PA_OK;
 }
@@ -239,7 +251,7 @@ pa_status enqueue_prep(pa_ctx *c, const DpParams &P, const ClassCfg &C, const ui
 {
     cudaStream_t st = c->stream;
     PA_CUDA(c, cudaMemsetAsync(c->hist.p, 0, sizeof(uint32_t) * kBuckets, st));
-    PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, st));
+    PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, st));
     PA_CUDA(c, cudaMemsetAsync(c->pstats.p, 0, sizeof(PrepStats), st));
     int cls_blocks = (int)std::min<uint64_t>((n_pairs * 32 + 127) / 128, (uint64_t)c->sm_count * 128);
     if (cls_blocks < 1) cls_blocks = 1;
@@ -266,9 +278,17 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
                   uint64_t n_pairs)
 {
     cudaStream_t st = c->stream;
-    uint32_t *counters = (uint32_t *)c->counters.p;   // [0..3] unit queues, [4] rerun count, [5] zero
+    // counters: [0..3] group queues, [4] rerun count, [5] zero, [6] long rerun count, [8] error
+    // bits, [9..12] CTA queues, [13..15] cluster queues, [16..21] routing of the largest pairs
+    uint32_t *counters = (uint32_t *)c->counters.p;
     pa_status ps = enqueue_prep(c, P, C, s1, o1, s2, o2, out, n_pairs);
     if (ps) return ps;
+    const int cl_grid = c->ring.p ? dp_cluster_grid(true, false, P.local ? M_LOCAL : M_GLOBAL, c->ring_grid) : 0;
+    if (c->ring.p) {
+        k_route_huge<<<1, 1, 0, st>>>((const uint32_t *)c->counts.p, (uint32_t)(cl_grid / kClusterBlocks),
+                                      counters + 16);
+        c->last_launches++;
+    }
 
     const int mode = P.local ? M_LOCAL : ((P.last_column_free || P.last_row_free) ? M_GLOBAL_FREE : M_GLOBAL);
     DpLaunch L;
@@ -289,6 +309,28 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
     // inside a capture the record must become a graph node to fire on every replay
     const unsigned ev_flags = capturing == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
     PA_CUDA(c, cudaEventRecordWithFlags(c->ev_dp0, st, ev_flags));
+    // the largest pairs first, on the side stream: clusters of blocks per pair; the kernels
+    // below fill the SMs those clusters leave free
+    DpLaunch LL = L;
+    if (c->ring.p) {
+        LL.ring = (Cell *)c->ring.p;
+        LL.ring_stride = (uint64_t)c->ring_m + 2;
+        LL.error = counters + 8;
+        LL.rerun_list = (uint32_t *)c->rerun_long.p;
+        LL.rerun_count = counters + 6;
+        LL.G = 32;
+        PA_CUDA(c, cudaEventRecord(c->ev_fork, st));
+        PA_CUDA(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+        DpLaunch LC = LL;
+        LC.ring = cluster_ring(c);
+        const Klass hc[3] = {K_S16H, K_S32H, K_GENH};
+        for (int k = 0; k < 3; ++k) {
+            LC.begin_ptr = ranges + hc[k]; LC.count_ptr = counters + 16 + k; LC.unit_counter = counters + 13 + k;
+            PA_CUDA(c, dp_cluster_launch(k == 0, k == 2, mode, dp_cluster_grid(k == 0, k == 2, mode, c->ring_grid),
+                                         c->side, LC, P));
+        }
+        PA_CUDA(c, cudaEventRecord(c->ev_join, c->side));
+    }
     // s16x2 class
     L.begin_ptr = ranges + K_S16; L.count_ptr = counts + K_S16; L.unit_counter = counters + 0; L.G = c->G[K_S16];
     launch_class(c, K_S16, mode, true, false, L, P);
@@ -300,18 +342,18 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
     launch_class(c, K_GEN, mode, false, true, L, P);
     // long pairs: whole blocks per pair; their s16 results that fail the check are redone in s32
     if (c->ring.p) {
-        DpLaunch LL = L;
-        LL.ring = (Cell *)c->ring.p;
-        LL.ring_stride = (uint64_t)c->ring_m + 2;
-        LL.error = counters + 8;
-        LL.rerun_list = (uint32_t *)c->rerun_long.p;
-        LL.rerun_count = counters + 6;
-        LL.G = 32;
-        const Klass lc[3] = {K_S16L, K_S32L, K_GENL};
+        const Klass lc[3] = {K_S16L, K_S32L, K_GENL}, hl[3] = {K_S16H, K_S32H, K_GENH};
         for (int k = 0; k < 3; ++k) {
             LL.begin_ptr = ranges + lc[k]; LL.count_ptr = counts + lc[k]; LL.unit_counter = counters + 9 + k;
+            LL.lead_order = (const uint32_t *)c->order.p;          // the largest pairs the router left here
+            LL.lead_begin_ptr = ranges + hl[k];
+            LL.lead_count_ptr = counters + 19 + k;
             dp_cta_launch(k == 0, k == 2, mode, c->ring_grid, st, LL, P);
         }
+        LL.lead_order = nullptr;
+        LL.lead_begin_ptr = nullptr;
+        LL.lead_count_ptr = nullptr;
+        PA_CUDA(c, cudaStreamWaitEvent(st, c->ev_join, 0));   // the cluster kernels' results and redo list
         if (mode != M_LOCAL) {
             LL.order = (const uint32_t *)c->rerun_long.p;
             LL.begin_ptr = counters + 5;
@@ -320,7 +362,7 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
             LL.rerun = 1;
             dp_cta_launch(false, false, mode, c->ring_grid, st, LL, P);
         }
-        c->last_launches += mode != M_LOCAL ? 4 : 3;
+        c->last_launches += mode != M_LOCAL ? 7 : 6;
     }
     // s16 global results that failed the exactness check, recomputed in s32
     if (mode != M_LOCAL) {
@@ -354,7 +396,8 @@ pa_status ensure_ring(pa_ctx *c, int64_t max_m)
     per_sm = std::max(per_sm, band_labels_cta_occupancy());
     const int grid = per_sm * c->sm_count;
     const int32_t m = (int32_t)std::max<int64_t>(max_m, c->ring_m);
-    pa_status s = ensure(c, c->ring, (size_t)grid * 8 * ((size_t)m + 2) * sizeof(Cell));
+    // two regions: CTA-mode blocks and cluster-mode blocks run at the same time
+    pa_status s = ensure(c, c->ring, (size_t)2 * grid * 8 * ((size_t)m + 2) * sizeof(Cell));
     if (s) return s;
     c->ring_m = m;
     c->ring_grid = grid;
@@ -375,7 +418,7 @@ pa_status prepare_buffers(pa_ctx *c, uint64_t n_pairs, uint64_t b1)
     if ((s = ensure(c, c->sums, sizeof(uint32_t) * 1024))) return s;
     if ((s = ensure(c, c->ranges, 64))) return s;
     if ((s = ensure(c, c->counts, 64))) return s;
-    if ((s = ensure(c, c->counters, 64))) return s;
+    if ((s = ensure(c, c->counters, 128))) return s;
     if ((s = ensure(c, c->pstats, sizeof(PrepStats)))) return s;
     if ((s = ensure(c, c->qtab, (b1 + np) * 4))) return s;
     if ((s = ensure(c, c->boundary, (b1 + np) * sizeof(Cell)))) return s;
@@ -455,13 +498,17 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     if ((s = prepare_buffers(c, n_pairs, b1))) return s;
     const uint64_t np = n_pairs;
     // the band work classes: {lanes16, cta} -> s16 groups, s32 groups, s16 blocks, s32 blocks
+    // the band work classes: s16x2 / s32 lanes x one group / one block / one cluster per unit
     struct BandClass {
-        bool lanes16, cta;
+        bool lanes16;
+        int kind;                 // 0 groups, 1 CTA mode, 2 cluster mode
         Klass klass;
         int rows;
     };
-    const BandClass bc[4] = {{true, false, K_S16, c->G[K_S16] * kR}, {false, false, K_S32, c->G[K_S32] * kR},
-                             {true, true, K_S16L, 32 * kR}, {false, true, K_S32L, 32 * kR}};
+    constexpr int NB = 6;
+    BandClass bc[NB] = {{true, 0, K_S16, c->G[K_S16] * kR}, {false, 0, K_S32, c->G[K_S32] * kR},
+                        {true, 1, K_S16L, 32 * kR},         {false, 1, K_S32L, 32 * kR},
+                        {true, 2, K_S16H, 32 * kR},         {false, 2, K_S32H, 32 * kR}};
     const int min_rows = std::min(std::min(bc[0].rows, bc[1].rows), 32 * kR);
     if ((s = ensure(c, c->band_spec, np * sizeof(BandSpec)))) return s;
     if ((s = ensure(c, c->band_win, (b2 / min_rows + np + 1) * sizeof(int2)))) return s;
@@ -475,7 +522,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     uint32_t *counters = (uint32_t *)c->counters.p;
     uint32_t *ctr = (uint32_t *)c->band_ctr.p;      // [0] zero, [1..31] totals and queues, [32..33] cells
     PA_CUDA(c, cudaEventRecord(c->ev0, st));
-    PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, st));
+    PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, st));
     PA_CUDA(c, cudaMemsetAsync(c->band_ctr.p, 0, 256, st));
     if ((s = enqueue_prep(c, P, C, s1, o1, s2, o2, out, np))) return s;
     BandSpec *spec = (BandSpec *)c->band_spec.p;
@@ -490,10 +537,15 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     } else if ((s = band_predict(c, P, s1, o1, s2, o2, np, spec))) {
         return s;
     }
-    uint32_t ranges[8], counts[8];
+    uint32_t ranges[16], counts[16];
     PA_CUDA(c, cudaMemcpyAsync(ranges, c->ranges.p, sizeof(ranges), cudaMemcpyDeviceToHost, st));
     PA_CUDA(c, cudaMemcpyAsync(counts, c->counts.p, 4 * kClasses, cudaMemcpyDeviceToHost, st));
     PA_CUDA(c, cudaStreamSynchronize(st));
+    // the largest pairs go to clusters only when their units fit in two waves of clusters
+    if (c->ring.p) {
+        const int slots = dp_cluster_grid(true, false, M_BAND, c->ring_grid) / kClusterBlocks;
+        if ((counts[K_S16H] + 1) / 2 + counts[K_S32H] > 2u * (uint32_t)slots) bc[4].kind = bc[5].kind = 1;
+    }
 
     DpLaunch L;
     std::memset(&L, 0, sizeof(L));
@@ -508,17 +560,23 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     L.ring = (Cell *)c->ring.p;
     L.ring_stride = (uint64_t)c->ring_m + 2;
     L.error = counters + 8;
-    // the full DP of a list: group kernels (with the s16 -> s32 redo list) or whole blocks
-    auto full_dp = [&](int k, const uint32_t *list, uint32_t *count_word, uint32_t *queue) {
+    // the full DP of a list: group kernels (with the s16 -> s32 redo list), whole blocks or clusters
+    auto full_dp = [&](int k, const uint32_t *list, uint32_t *count_word, uint32_t *queue) -> pa_status {
         DpLaunch F = L;
         F.order = list;
         F.begin_ptr = ctr + 0;
         F.count_ptr = count_word;
         F.unit_counter = queue;
         F.rerun = 0;
-        F.rerun_list = (uint32_t *)(bc[k].cta ? c->rerun_long.p : c->rerun.p);
-        F.rerun_count = counters + (bc[k].cta ? 6 : 4);
-        if (bc[k].cta) {
+        F.rerun_list = (uint32_t *)(bc[k].kind ? c->rerun_long.p : c->rerun.p);
+        F.rerun_count = counters + (bc[k].kind ? 6 : 4);
+        if (bc[k].kind == 2) {
+            F.G = 32;
+            F.ring = cluster_ring(c);
+            PA_CUDA(c, dp_cluster_launch(bc[k].lanes16, false, M_GLOBAL,
+                                         dp_cluster_grid(bc[k].lanes16, false, M_GLOBAL, c->ring_grid), st, F, P));
+            c->last_launches++;
+        } else if (bc[k].kind == 1) {
             F.G = 32;
             dp_cta_launch(bc[k].lanes16, false, M_GLOBAL, c->ring_grid, st, F, P);
             c->last_launches++;
@@ -526,6 +584,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
             F.G = c->G[bc[k].klass];
             launch_class(c, bc[k].klass, M_GLOBAL, bc[k].lanes16, false, F, P);
         }
+        return PA_OK;
     };
     // byte-compare classes: the full DP
     {
@@ -543,18 +602,34 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
             F.count_ptr = (const uint32_t *)c->counts.p + K_GENL;
             F.unit_counter = counters + 11;
             F.G = 32;
+            F.rerun_list = (uint32_t *)c->rerun_long.p;
+            F.rerun_count = counters + 6;
             dp_cta_launch(false, true, M_GLOBAL, c->ring_grid, st, F, P);
+            c->last_launches++;
+        }
+        if (counts[K_GENH]) {
+            F.begin_ptr = (const uint32_t *)c->ranges.p + K_GENH;
+            F.count_ptr = (const uint32_t *)c->counts.p + K_GENH;
+            F.unit_counter = counters + 15;
+            F.G = 32;
+            F.ring = cluster_ring(c);
+            F.rerun_list = (uint32_t *)c->rerun_long.p;
+            F.rerun_count = counters + 6;
+            PA_CUDA(c, dp_cluster_launch(false, true, M_GLOBAL, dp_cluster_grid(false, true, M_GLOBAL, c->ring_grid),
+                                         st, F, P));
             c->last_launches++;
         }
     }
 
-    uint32_t *lst[16];
-    for (int k = 0; k < 16; ++k) lst[k] = (uint32_t *)c->band_list[k].p;
-    uint32_t *cur[4] = {lst[0], lst[1], lst[2], lst[3]}, *nxt[4] = {lst[4], lst[5], lst[6], lst[7]},
-             *full[4] = {lst[8], lst[9], lst[10], lst[11]};
-    uint32_t *tmp = lst[12], *redo = lst[13];
-    uint32_t ncur[4], nfull[4] = {0, 0, 0, 0};
-    for (int k = 0; k < 4; ++k) {
+    uint32_t *cur[NB], *nxt[NB], *full[NB];
+    for (int k = 0; k < NB; ++k) {
+        cur[k] = (uint32_t *)c->band_list[k].p;
+        nxt[k] = (uint32_t *)c->band_list[NB + k].p;
+        full[k] = (uint32_t *)c->band_list[2 * NB + k].p;
+    }
+    uint32_t *tmp = (uint32_t *)c->band_list[3 * NB].p, *redo = (uint32_t *)c->band_list[3 * NB + 1].p;
+    uint32_t ncur[NB], nfull[NB] = {};
+    for (int k = 0; k < NB; ++k) {
         ncur[k] = counts[bc[k].klass];
         if (ncur[k])
             PA_CUDA(c, cudaMemcpyAsync(cur[k], (const uint32_t *)c->order.p + ranges[bc[k].klass], ncur[k] * 4ull,
@@ -584,12 +659,18 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         L.begin_ptr = ctr + 0;
         L.count_ptr = ctr + 2;
         L.unit_counter = ctr + 3;
-        L.G = B.cta ? 32 : c->G[B.klass];
+        L.G = B.kind ? 32 : c->G[B.klass];
         L.band_rows = B.rows;
         L.band_round = r;
         L.rerun = rerun ? 1 : 0;
-        band_dp_launch(B.lanes16, B.cta, B.cta ? c->ring_grid : band_dp_occupancy(B.lanes16, false) * c->sm_count,
-                       st, L, P);
+        if (B.kind == 2) {
+            DpLaunch LB = L;
+            LB.ring = cluster_ring(c);
+            PA_CUDA(c, dp_cluster_launch(B.lanes16, false, M_BAND, dp_cluster_grid(B.lanes16, false, M_BAND, c->ring_grid),
+                                         st, LB, P));
+        } else
+            band_dp_launch(B.lanes16, B.kind == 1,
+                           B.kind ? c->ring_grid : band_dp_occupancy(B.lanes16, false) * c->sm_count, st, L, P);
         compact_launch(st, tmp, code, nb, 1, bsum, next + n_next, ctr + 4);
         compact_launch(st, tmp, code, nb, 3, bsum, redo_out ? redo_out : tmp, ctr + 5);
         c->last_launches += 7;
@@ -601,11 +682,15 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         banded += nb - h[0] - h[1];
         return PA_OK;
     };
-    auto open_pairs = [&]() { return ncur[0] + ncur[1] + ncur[2] + ncur[3]; };
+    auto open_pairs = [&]() {
+        uint32_t t = 0;
+        for (int k = 0; k < NB; ++k) t += ncur[k];
+        return t;
+    };
     for (int r = 0; r < c->band_opt.max_rounds && open_pairs(); ++r) {
         ++rounds;
-        uint32_t nn[4] = {0, 0, 0, 0};
-        for (int k16 : {0, 2}) {                      // s16 classes, then their s32 redo, then s32
+        uint32_t nn[NB] = {};
+        for (int k16 : {0, 2, 4}) {                   // s16 classes, then their s32 redo, then s32
             uint32_t nredo = 0, none = 0;
             if (ncur[k16] && (s = band_step(k16, cur[k16], ncur[k16], r, false, nxt[k16], nn[k16], redo, nredo)))
                 return s;
@@ -615,22 +700,22 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
                 (s = band_step(k16 + 1, cur[k16 + 1], ncur[k16 + 1], r, false, nxt[k16 + 1], nn[k16 + 1], nullptr, none)))
                 return s;
         }
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < NB; ++k) {
             std::swap(cur[k], nxt[k]);
             ncur[k] = nn[k];
         }
     }
     // still open after the last round: full DP
-    uint32_t hc[8];
-    for (int k = 0; k < 4; ++k) {
+    uint32_t hc[NB];
+    for (int k = 0; k < NB; ++k) {
         if (ncur[k])
             PA_CUDA(c, cudaMemcpyAsync(full[k] + nfull[k], cur[k], ncur[k] * 4ull, cudaMemcpyDeviceToDevice, st));
         nfull[k] += ncur[k];
         hc[k] = nfull[k];
     }
-    PA_CUDA(c, cudaMemcpyAsync(ctr + 6, hc, 16, cudaMemcpyHostToDevice, st));
-    for (int k = 0; k < 4; ++k)
-        if (nfull[k]) full_dp(k, full[k], ctr + 6 + k, ctr + 10 + k);
+    PA_CUDA(c, cudaMemcpyAsync(ctr + 6, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
+    for (int k = 0; k < NB; ++k)
+        if (nfull[k] && (s = full_dp(k, full[k], ctr + 6 + k, ctr + 16 + k))) return s;
     if (nfull[0]) {                                   // s16 group results that failed their check
         DpLaunch F = L;
         F.order = (const uint32_t *)c->rerun.p;
@@ -641,7 +726,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         F.G = c->G[K_S32];
         launch_class(c, K_S32, M_GLOBAL, false, false, F, P);
     }
-    if (nfull[2]) {                                   // the same for s16 long pairs
+    if (nfull[2] || nfull[4]) {                       // the same for s16 long and largest pairs
         DpLaunch F = L;
         F.order = (const uint32_t *)c->rerun_long.p;
         F.begin_ptr = counters + 5;
@@ -667,7 +752,8 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     st_out->kernel_launches = c->last_launches;
     st_out->dp_ms = st_out->device_ms;
     st_out->pairs_banded = banded;
-    st_out->pairs_full_dp = nfull[0] + nfull[1] + nfull[2] + nfull[3] + counts[K_GEN] + counts[K_GENL];
+    st_out->pairs_full_dp = counts[K_GEN] + counts[K_GENL] + counts[K_GENH];
+    for (int k = 0; k < NB; ++k) st_out->pairs_full_dp += nfull[k];
     st_out->band_cells = cells;
     st_out->band_rounds = rounds;
     return s;
@@ -688,9 +774,9 @@ pa_status read_stats(pa_ctx *c, pa_stats *stats)
         cudaGetLastError();
         const uint64_t rr = (uint64_t)ctr[4] + ctr[6];
         stats->cells = ps.cells;
-        stats->pairs_s16 = ps.n_class[K_S16] + ps.n_class[K_S16L] - rr;
-        stats->pairs_s32 = ps.n_class[K_S32] + ps.n_class[K_S32L] + rr;
-        stats->pairs_general = ps.n_class[K_GEN] + ps.n_class[K_GENL];
+        stats->pairs_s16 = ps.n_class[K_S16] + ps.n_class[K_S16L] + ps.n_class[K_S16H] - rr;
+        stats->pairs_s32 = ps.n_class[K_S32] + ps.n_class[K_S32L] + ps.n_class[K_S32H] + rr;
+        stats->pairs_general = ps.n_class[K_GEN] + ps.n_class[K_GENL] + ps.n_class[K_GENH];
         stats->pairs_trivial = ps.n_class[K_NONE];
         stats->pairs_rerun = rr;
     }
@@ -741,7 +827,7 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
             if (ce != cudaSuccess) return fail(c, PA_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ce));
             it = c->graphs.emplace(key, ex).first;
         } else {
-            c->last_launches = 6 + 3 + (P.local ? 0 : 1) + (c->ring.p ? (P.local ? 3 : 4) : 0);
+            c->last_launches = 6 + 3 + (P.local ? 0 : 1) + (c->ring.p ? (P.local ? 7 : 8) : 0);
         }
         PA_CUDA(c, cudaGraphLaunch(it->second, c->stream));
     } else {
@@ -844,7 +930,10 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
         cudaEventCreate(&c->ev2) != cudaSuccess || cudaEventCreate(&c->ev3) != cudaSuccess ||
-        cudaEventCreate(&c->ev_dp0) != cudaSuccess || cudaEventCreate(&c->ev_dp1) != cudaSuccess) {
+        cudaEventCreate(&c->ev_dp0) != cudaSuccess || cudaEventCreate(&c->ev_dp1) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
         delete c;
         return PA_ERR_CUDA;
@@ -892,6 +981,9 @@ pa_status pa_destroy(pa_ctx *c)
     if (c->ev3) cudaEventDestroy(c->ev3);
     if (c->ev_dp0) cudaEventDestroy(c->ev_dp0);
     if (c->ev_dp1) cudaEventDestroy(c->ev_dp1);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return PA_OK;
@@ -950,6 +1042,16 @@ pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells)
     if (!ctx) return PA_ERR_INVALID_ARGUMENT;
     ctx->long_cells = cells > (uint64_t)INT64_MAX ? INT64_MAX : (int64_t)std::max<uint64_t>(cells, 1);
     for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);   // the classifier's rule changed
+    ctx->graphs.clear();
+    return PA_OK;
+}
+
+pa_status pa_set_cluster_threshold(pa_ctx *ctx, uint64_t cells, uint32_t min_rows)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    ctx->huge_cells = cells > (uint64_t)INT64_MAX ? INT64_MAX : (int64_t)std::max<uint64_t>(cells, 1);
+    ctx->huge_min_n = (int32_t)std::min<uint32_t>(std::max<uint32_t>(min_rows, 1), 1u << 30);
+    for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
     ctx->graphs.clear();
     return PA_OK;
 }

@@ -20,12 +20,18 @@ struct DpParams {
 };
 
 // Work classes produced by the classifier; the class is the top field of the bucket key.
-// Classes 4..6 are the long-pair versions of 0..2, computed by whole blocks (CTA mode).
-enum Klass : uint32_t { K_S16 = 0, K_S32 = 1, K_GEN = 2, K_NONE = 3, K_S16L = 4, K_S32L = 5, K_GENL = 6 };
-constexpr int kClasses = 7;
+// Classes 4..6 are the long-pair versions of 0..2, computed by whole blocks (CTA mode);
+// 8..10 the largest pairs, computed by thread-block clusters (cluster mode).
+enum Klass : uint32_t {
+    K_S16 = 0, K_S32 = 1, K_GEN = 2, K_NONE = 3, K_S16L = 4, K_S32L = 5, K_GENL = 6,
+    K_S16H = 8, K_S32H = 9, K_GENH = 10
+};
+constexpr int kClasses = 11;
 constexpr uint32_t kLongOffset = 4;
+constexpr uint32_t kHugeOffset = 8;
+constexpr int kClusterBlocks = 4;            // blocks per cluster in cluster mode
 
-constexpr int kKeyBits = 19;                 // 3 class | 6 pass | 10 length bits
+constexpr int kKeyBits = 20;                 // 4 class | 6 pass | 10 length bits
 constexpr uint32_t kBuckets = 1u << kKeyBits;
 constexpr int kClassShift = 16;
 
@@ -75,6 +81,10 @@ struct DpLaunch {
     int32_t *band_ub;             // optional: the largest exit bound per pair
     int32_t band_rows;            // rows per pass of the window table (G * R)
     int32_t band_round;
+    // CTA mode: an optional list taken before `order` (the largest pairs, largest first)
+    const uint32_t *lead_order;
+    const uint32_t *lead_begin_ptr;
+    const uint32_t *lead_count_ptr;
     // CTA mode (long pairs): each block owns ring rows of ring_stride cells, one per group
     Cell *ring;
     uint64_t ring_stride;

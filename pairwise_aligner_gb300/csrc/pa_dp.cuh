@@ -41,6 +41,7 @@
 //   global -- H(m, n) is read where it is computed; free trailing gaps also
 //             scan the last row (i = m) and the last column (j = n).
 #pragma once
+#include <cooperative_groups.h>
 #include <cuda/atomic>
 
 #include "pa_common.cuh"
@@ -168,11 +169,26 @@ struct GroupWork {
 constexpr uint32_t kSpinLimit = 1u << 24;
 constexpr uint32_t kErrWaitTimeout = 1u;
 
+// SYNC scope of a kernel: 0 none (one group per pair), 1 the block (CTA mode), 2 the
+// thread-block cluster (cluster mode: flags may live in another block's shared memory).
+__device__ __forceinline__ int load_acquire_cluster(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.cluster.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void store_release_cluster(int *p, int v)
+{
+    asm volatile("st.release.cluster.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <int SCOPE>
 __device__ __forceinline__ int32_t wait_progress(int *flag, int32_t need, uint32_t *err)
 {
-    cuda::atomic_ref<int, cuda::thread_scope_block> a(*flag);
     for (uint32_t it = 0; it < kSpinLimit; ++it) {
-        const int v = a.load(cuda::memory_order_acquire);
+        const int v = SCOPE == 2 ? load_acquire_cluster(flag)
+                                 : cuda::atomic_ref<int, cuda::thread_scope_block>(*flag).load(cuda::memory_order_acquire);
         if (v >= need) return v;
         if (it >= 64) __nanosleep(64);
     }
@@ -180,9 +196,23 @@ __device__ __forceinline__ int32_t wait_progress(int *flag, int32_t need, uint32
     return INT32_MAX;
 }
 
+template <int SCOPE>
 __device__ __forceinline__ void publish_progress(int *flag, int32_t v)
 {
-    cuda::atomic_ref<int, cuda::thread_scope_block>(*flag).store(v, cuda::memory_order_release);
+    if (SCOPE == 2) store_release_cluster(flag, v);
+    else cuda::atomic_ref<int, cuda::thread_scope_block>(*flag).store(v, cuda::memory_order_release);
+}
+
+// A boundary cell written by another pass: in cluster mode the writer may sit on another SM,
+// so the read goes to L2 (no stale L1 line of an earlier pass that used the same ring row).
+template <int SCOPE>
+__device__ __forceinline__ Cell load_cell(const Cell *p)
+{
+    if (SCOPE == 2) {
+        const uint2 v = __ldcg(reinterpret_cast<const uint2 *>(p));
+        return Cell{v.x, v.y};
+    }
+    return *p;
 }
 
 // Upper bound on the score of a path that enters cell (i, j) from inside the band
@@ -213,7 +243,7 @@ __device__ __forceinline__ uint32_t stored(const GroupWork &w, int32_t true_valu
 
 // VAR bit 0: short-chain form of the vertical gap; bit 2: branch-free top input for
 // thread 0 and an L1 prefetch of the score tables eight columns ahead.
-template <class V, int R, int RA, int MODE, bool GEN, int VAR, bool SYNC = false>
+template <class V, int R, int RA, int MODE, bool GEN, int VAR, int SYNC = 0>
 __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, GroupWork &w, int p, int t, int G,
                                          unsigned gmask, uint4 *snap)
 {
@@ -279,15 +309,34 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             b = NL == 2 ? __ldg(w.qt[1] + min(col - 1, w.m[1])) : a;
         }
     };
-    Cell nbuf = Cell{0u, 0u};                        // thread 0, pass > 0: next boundary cell
+    // thread 0, pass > 0: the next boundary cell (and in cluster mode, where the cell comes
+    // from L2, the one after it as well)
+    constexpr bool PF2 = SYNC == 2;
+    Cell nbuf = Cell{0u, 0u}, nbuf2 = Cell{0u, 0u};
     // thread 0 of a pass below the first reads the boundary row; in CTA mode it first
     // waits until the pass above has published the column
     auto ready = [&](int32_t col) {
-        if (SYNC && w.seen < w.base_in + col) w.seen = wait_progress(w.prog_in, w.base_in + col, L.error);
+        if (SYNC && w.seen < w.base_in + col) w.seen = wait_progress<SYNC>(w.prog_in, w.base_in + col, L.error);
+    };
+    auto advance = [&](int32_t i) {                  // at column i < iend: fetch what column i + 1 needs
+        if (PF2) {
+            nbuf = nbuf2;
+            if (i + 2 <= iend) {
+                ready(i + 2);
+                nbuf2 = load_cell<SYNC>(w.bin + i + 2);
+            }
+        } else {
+            ready(i + 1);
+            nbuf = load_cell<SYNC>(w.bin + i + 1);
+        }
     };
     if (t == 0 && p > 0) {
         ready(ibase + 1);
-        nbuf = w.bin[ibase + 1];
+        nbuf = load_cell<SYNC>(w.bin + ibase + 1);
+        if (PF2 && ibase + 2 <= iend) {
+            ready(ibase + 2);
+            nbuf2 = load_cell<SYNC>(w.bin + ibase + 2);
+        }
     }
     constexpr bool TUNED = (VAR & 4) != 0;
     const bool first_thread = t == 0;
@@ -302,10 +351,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             const uint32_t nt = V::max2(V::subc(topH, i == 1 ? step1 : stepn), CLAMP);
             topH = top_border ? nt : topH;
             const Cell c = nbuf;
-            if (top_buffer && i < iend) {
-                ready(i + 1);
-                nbuf = w.bin[i + 1];
-            }
+            if (top_buffer && i < iend) advance(i);
             upH = top_border ? nt : (top_buffer ? c.h : upH);
             upE = top_border ? V::subc(nt, GOEA) : (top_buffer ? c.e : upE);
             if (!GEN && i + 8 <= iend) {
@@ -320,10 +366,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             } else {
                 upH = nbuf.h;
                 upE = nbuf.e;
-                if (i < iend) {
-                    ready(i + 1);
-                    nbuf = w.bin[i + 1];
-                }
+                if (i < iend) advance(i);
             }
         }
         if (BAND && i == iend) top_last = upH;
@@ -369,7 +412,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
         outE = Ed;
         if (t == G - 1 && !last_pass) {
             w.bout[i] = Cell{outH, outE};
-            if (SYNC && ((i & 7) == 0 || i == iend)) publish_progress(w.prog_out, w.base_out + i);
+            if (SYNC && ((i & 7) == 0 || i == iend)) publish_progress<SYNC>(w.prog_out, w.base_out + i);
         }
 
         if (MODE == M_LABEL_FWD || MODE == M_LABEL_REV) {
@@ -579,7 +622,7 @@ __device__ __forceinline__ int2 band_window(const DpLaunch &L, const GroupWork &
 
 // One pass p of the group's pair(s): the band window and its exits (band mode),
 // then the wavefront sweep.
-template <class V, int R, int MODE, bool GEN, int VAR, bool SYNC>
+template <class V, int R, int MODE, bool GEN, int VAR, int SYNC>
 __device__ __forceinline__ void pass_body(const DpLaunch &L, const DpParams &P, GroupWork &w, int p, int t, int G,
                                           unsigned gmask, uint4 *snap)
 {
@@ -600,8 +643,8 @@ __device__ __forceinline__ void pass_body(const DpLaunch &L, const DpParams &P, 
         const int32_t c0 = bcur.x - 1;
         w.diag0 = NEGV;
         if (t == 0 && p > 0 && c0 >= bprev.x && c0 <= bprev.y) {
-            if (SYNC && w.seen < w.base_in + c0) w.seen = wait_progress(w.prog_in, w.base_in + c0, L.error);
-            w.diag0 = w.bin[c0].h;
+            if (SYNC && w.seen < w.base_in + c0) w.seen = wait_progress<SYNC>(w.prog_in, w.base_in + c0, L.error);
+            w.diag0 = load_cell<SYNC>(w.bin + c0).h;
         }
     }
     switch (rpt / kChunk) {
@@ -757,7 +800,7 @@ __global__ void __launch_bounds__(kBlock, MINB) dp_kernel(DpLaunch L, DpParams P
         if (first >= count) continue;                // idle group in the last unit
         GroupWork w;
         init_work<V, MODE>(L, P, order, first, count, G, R, w);
-        for (int p = 0; p < w.passes; ++p) pass_body<V, R, MODE, GEN, VAR, false>(L, P, w, p, t, G, gmask, snap_store);
+        for (int p = 0; p < w.passes; ++p) pass_body<V, R, MODE, GEN, VAR, 0>(L, P, w, p, t, G, gmask, snap_store);
         reduce_group<V, MODE>(w, gmask, G);
         if (t == 0) emit<V, MODE>(L, P, w, first);
         __syncwarp(gmask);
@@ -785,9 +828,12 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cta(DpLaunch L, DpParams 
     __shared__ unsigned long long s_cells[NG];
     const int t = threadIdx.x & 31, g = threadIdx.x >> 5;
     const unsigned gmask = 0xffffffffu;
-    const uint32_t count = *L.count_ptr;
-    const uint32_t *order = L.order + *L.begin_ptr;
-    const uint32_t n_units = (count + NL - 1) / NL;
+    const uint32_t count_main = *L.count_ptr;
+    const uint32_t *order_main = L.order + *L.begin_ptr;
+    const uint32_t count_lead = L.lead_count_ptr ? *L.lead_count_ptr : 0u;
+    const uint32_t *order_lead = L.lead_count_ptr ? L.lead_order + *L.lead_begin_ptr : nullptr;
+    const uint32_t units_lead = (count_lead + NL - 1) / NL;
+    const uint32_t n_units = units_lead + (count_main + NL - 1) / NL;
     Cell *ring = L.ring + (uint64_t)blockIdx.x * NG * L.ring_stride;
 
     for (;;) {
@@ -797,7 +843,11 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cta(DpLaunch L, DpParams 
         uint32_t u = s_unit;
         __syncthreads();
         if (u >= n_units) break;
-        u = n_units - 1 - u;                         // largest shapes first
+        // the lead list first, then the main list, each largest shapes first
+        const bool lead = u < units_lead;
+        const uint32_t count = lead ? count_lead : count_main;
+        const uint32_t *order = lead ? order_lead : order_main;
+        u = lead ? units_lead - 1 - u : n_units - 1 - u;
         const uint32_t first = u * NL;
         GroupWork w;
         init_work<V, MODE>(L, P, order, first, count, G, R, w);
@@ -810,8 +860,8 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cta(DpLaunch L, DpParams 
             w.base_in = (p - 1) * span;
             w.base_out = p * span;
             w.seen = INT32_MIN;
-            pass_body<V, R, MODE, GEN, VAR, true>(L, P, w, p, t, G, gmask, snap_store);
-            if (t == G - 1 && p + 1 < w.passes) publish_progress(w.prog_out, w.base_out + w.ms + 1);
+            pass_body<V, R, MODE, GEN, VAR, 1>(L, P, w, p, t, G, gmask, snap_store);
+            if (t == G - 1 && p + 1 < w.passes) publish_progress<1>(w.prog_out, w.base_out + w.ms + 1);
         }
         reduce_group<V, MODE>(w, gmask, G);
         if (t == 0) {
@@ -846,4 +896,109 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cta(DpLaunch L, DpParams 
     }
 }
 
+// Cluster mode for the largest pairs: a cluster of CL blocks (co-scheduled by the
+// hardware) works on one unit with all its 8*CL warps, pass p on group p % (8*CL)
+// (block (p % (8*CL)) / 8, warp p % 8).  Progress flags stay in the shared memory
+// of the producing block and are read through distributed shared memory with
+// cluster-scope acquire; ring rows are the 8*CL rows of the cluster's blocks.
+template <class V, int R, int MODE, bool GEN, int VAR, int CL>
+__global__ void __launch_bounds__(kBlock, 2) dp_kernel_cluster(DpLaunch L, DpParams P)
+{
+    static_assert(R % kChunk == 0 && R <= 32, "R must be a multiple of the chunk");
+    constexpr int NL = V::LANES;
+    constexpr int NW = kBlock / 32;              // warps (groups) per block
+    constexpr int NG = NW * CL;                  // groups per cluster
+    constexpr int G = 32;
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    __shared__ uint4 snap_store[MODE == M_LOCAL ? NL * (R / 4) * kBlock : 1];
+    __shared__ int prog[NW];
+    __shared__ uint32_t s_unit;
+    __shared__ int32_t s_cand[NW][2][4];
+    __shared__ int32_t s_lb[NW][8][2];
+    __shared__ unsigned long long s_cells[NW];
+    __shared__ int32_t s_part[2][4];             // this block's merged result, read by rank 0
+    __shared__ int32_t s_plb[8][2];
+    __shared__ unsigned long long s_pcells;
+    const int t = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const unsigned gmask = 0xffffffffu;
+    const uint32_t count = *L.count_ptr;
+    const uint32_t *order = L.order + *L.begin_ptr;
+    const uint32_t n_units = (count + NL - 1) / NL;
+    Cell *ring = L.ring + (uint64_t)(blockIdx.x - rank) * NW * L.ring_stride;   // the cluster's rows
+    const int gg = rank * NW + g;                // this warp's group in the cluster
+
+    for (;;) {
+        if (threadIdx.x < NW) prog[threadIdx.x] = -1;
+        if (rank == 0 && threadIdx.x == 0) s_unit = atomicAdd(L.unit_counter, 1u);
+        cluster.sync();
+        uint32_t u = *cluster.map_shared_rank(&s_unit, 0);
+        cluster.sync();
+        if (u >= n_units) break;
+        u = n_units - 1 - u;                     // largest shapes first
+        const uint32_t first = u * NL;
+        GroupWork w;
+        init_work<V, MODE>(L, P, order, first, count, G, R, w);
+        const int32_t span = w.ms + 2;
+        for (int p = gg; p < w.passes; p += NG) {
+            const int pg = (p + NG - 1) % NG;    // the group of pass p - 1
+            w.bin = ring + (uint64_t)pg * L.ring_stride;
+            w.bout = ring + (uint64_t)(p % NG) * L.ring_stride;
+            w.prog_in = cluster.map_shared_rank(prog, pg / NW) + (pg % NW);
+            w.prog_out = &prog[g];
+            w.base_in = (p - 1) * span;
+            w.base_out = p * span;
+            w.seen = INT32_MIN;
+            pass_body<V, R, MODE, GEN, VAR, 2>(L, P, w, p, t, G, gmask, snap_store);
+            if (t == G - 1 && p + 1 < w.passes) publish_progress<2>(w.prog_out, w.base_out + w.ms + 1);
+        }
+        reduce_group<V, MODE>(w, gmask, G);
+        if (t == 0) {
+            for (int l = 0; l < 2; ++l) {
+                s_cand[g][l][0] = w.cs[l];
+                s_cand[g][l][1] = w.ci[l];
+                s_cand[g][l][2] = w.cj[l];
+                s_cand[g][l][3] = w.ub[l];
+            }
+            for (int c = 0; c < 8; ++c) { s_lb[g][c][0] = w.lb_v[c]; s_lb[g][c][1] = w.lb_j[c]; }
+            s_cells[g] = w.cells;
+        }
+        __syncthreads();
+        // merge the block's groups, then rank 0 merges the blocks
+        auto merge = [&](const int32_t (*cand)[4], const int32_t (*lb)[2], unsigned long long cells) {
+            for (int l = 0; l < 2; ++l) {
+                const int32_t *c = cand[l];
+                if (better(c[0], c[1], c[2], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = c[0]; w.ci[l] = c[1]; w.cj[l] = c[2]; }
+                w.ub[l] = max(w.ub[l], c[3]);
+            }
+            for (int c = 0; c < 8; ++c) {
+                const int32_t ov = lb[c][0], oj = lb[c][1];
+                if (ov > w.lb_v[c] || (ov == w.lb_v[c] && oj < w.lb_j[c])) { w.lb_v[c] = ov; w.lb_j[c] = oj; }
+            }
+            w.cells += cells;
+        };
+        if (threadIdx.x == 0) {
+            for (int k = 1; k < NW; ++k) merge(s_cand[k], s_lb[k], s_cells[k]);
+            for (int l = 0; l < 2; ++l) {
+                s_part[l][0] = w.cs[l];
+                s_part[l][1] = w.ci[l];
+                s_part[l][2] = w.cj[l];
+                s_part[l][3] = w.ub[l];
+            }
+            for (int c = 0; c < 8; ++c) { s_plb[c][0] = w.lb_v[c]; s_plb[c][1] = w.lb_j[c]; }
+            s_pcells = w.cells;
+        }
+        cluster.sync();
+        if (rank == 0 && threadIdx.x == 0) {
+            for (int r = 1; r < CL; ++r)
+                merge(cluster.map_shared_rank(s_part, r), cluster.map_shared_rank(s_plb, r),
+                      *cluster.map_shared_rank(&s_pcells, r));
+            emit<V, MODE>(L, P, w, first);
+        }
+        cluster.sync();
+    }
+}
+
 }  // namespace pa
+

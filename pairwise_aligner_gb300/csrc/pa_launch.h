@@ -18,4 +18,10 @@ int dp_cta_occupancy(bool lanes16, bool gen, int mode);
 void dp_cta_launch(bool lanes16, bool gen, int mode, int grid, cudaStream_t stream, const DpLaunch &L,
                    const DpParams &P);
 
+// Cluster mode (the largest pairs): clusters of kClusterBlocks blocks per pair; the grid is a
+// multiple of the cluster size and L.ring holds grid * 8 rows.  mode may be M_BAND.
+int dp_cluster_grid(bool lanes16, bool gen, int mode, int max_blocks);
+cudaError_t dp_cluster_launch(bool lanes16, bool gen, int mode, int grid, cudaStream_t stream, const DpLaunch &L,
+                              const DpParams &P);
+
 }  // namespace pa

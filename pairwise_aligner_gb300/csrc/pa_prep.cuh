@@ -18,13 +18,14 @@ struct ClassCfg {
     int32_t gcnt[kClasses];  // G of each class (for the last-pass chunk count)
     int32_t rpt[kClasses];   // R of each class
     int64_t long_cells;      // pairs with m*n at least this (and m <= long_max_m) go to CTA mode
-    int32_t long_max_m;      // the longest sequence1 the CTA ring rows hold
-    int32_t pad;
+    int64_t huge_cells;      // ... and with m*n at least this and n >= huge_min_n to cluster mode
+    int32_t long_max_m;      // the longest sequence1 the ring rows hold
+    int32_t huge_min_n;
 };
 
 struct PrepStats {
     unsigned long long cells;
-    unsigned long long n_class[8];
+    unsigned long long n_class[16];
     unsigned long long overflow;    // pairs whose int32 bound fails
 };
 
@@ -82,7 +83,7 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
     const uint32_t match4 = (uint8_t)(P.match - P.shift) * 0x01010101u;     // scores of H - shift * column
     const uint32_t mis4 = (uint8_t)(P.mismatch - P.shift) * 0x01010101u;
     // statistics are summed per lane 0 and per block, then added once per block
-    unsigned long long my_cells = 0, my_class[8] = {0, 0, 0, 0, 0, 0, 0, 0}, my_overflow = 0;
+    unsigned long long my_cells = 0, my_class[16] = {}, my_overflow = 0;
     for (uint64_t p = warp; p < n_pairs; p += nwarps) {
         const uint64_t q0 = off1[p], t0 = off2[p];
         const int64_t m = (int64_t)(off1[p + 1] - q0), n = (int64_t)(off2[p + 1] - t0);
@@ -104,8 +105,10 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
         // the clamp floor (checked after the DP), so any length may try s16 first
         else if (!C.force32 && C.s16_params && (!C.local || (int64_t)P.smax * min(m, n) <= 30000)) klass = K_S16;
         else klass = K_S32;
-        if (klass != K_NONE && m * n >= C.long_cells && m <= C.long_max_m && n <= (1 << 20)) klass += kLongOffset;
-        if (klass == K_S16 || klass == K_S32 || klass == K_S16L || klass == K_S32L) {
+        if (klass != K_NONE && m * n >= C.long_cells && m <= C.long_max_m && n <= (1 << 20))
+            klass += (m * n >= C.huge_cells && n >= C.huge_min_n) ? kHugeOffset : kLongOffset;
+        if (klass == K_S16 || klass == K_S32 || klass == K_S16L || klass == K_S32L || klass == K_S16H ||
+            klass == K_S32H) {
             uint32_t *qt = qtab + q0 + p;
             for (int64_t i = 4 * lane; i <= m; i += 128) {
                 const uint8_t *a = seq1 + q0 + i;
@@ -141,21 +144,21 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
             ++my_class[klass];
         }
     }
-    __shared__ unsigned long long sh[10];
-    if (threadIdx.x < 10) sh[threadIdx.x] = 0;
+    __shared__ unsigned long long sh[18];
+    if (threadIdx.x < 18) sh[threadIdx.x] = 0;
     __syncthreads();
     if (lane == 0) {
         if (my_cells) atomicAdd(&sh[0], my_cells);
-        for (int k = 0; k < 8; ++k)
+        for (int k = 0; k < 16; ++k)
             if (my_class[k]) atomicAdd(&sh[1 + k], my_class[k]);
-        if (my_overflow) atomicAdd(&sh[9], my_overflow);
+        if (my_overflow) atomicAdd(&sh[17], my_overflow);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         if (sh[0]) atomicAdd(&st->cells, sh[0]);
-        for (int k = 0; k < 8; ++k)
+        for (int k = 0; k < 16; ++k)
             if (sh[1 + k]) atomicAdd(&st->n_class[k], sh[1 + k]);
-        if (sh[9]) atomicAdd(&st->overflow, sh[9]);
+        if (sh[17]) atomicAdd(&st->overflow, sh[17]);
     }
 }
 
@@ -223,7 +226,7 @@ __global__ void k_scatter(const uint32_t *__restrict__ keys, uint64_t n_pairs, u
 {
     const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (p == 0) {
-        // class sizes from the class begins (class 7 holds no keys: ranges[7] is the end)
+        // class sizes from the class begins (classes 7 and 11.. hold no keys)
         for (int c = 0; c < kClasses; ++c) counts[c] = ranges[c + 1] - ranges[c];
     }
     if (p >= n_pairs) return;
@@ -231,6 +234,23 @@ __global__ void k_scatter(const uint32_t *__restrict__ keys, uint64_t n_pairs, u
     if ((key >> kClassShift) == K_NONE) return;
     const uint32_t pos = atomicAdd(&cursor[key], 1u);
     order[pos] = (uint32_t)p;
+}
+
+// Who computes the largest pairs: clusters of blocks when their units fit in two waves of
+// the clusters that can be resident (their run time would otherwise be one block's), else
+// the CTA-mode kernel, ahead of the long pairs (more units than clusters: blocks, which
+// quantise a pair's passes more finely, keep the GPU as busy).  words[0..2] are the
+// cluster kernels' counts of K_S16H, K_S32H, K_GENH, words[3..5] the CTA kernels' lead counts.
+__global__ void k_route_huge(const uint32_t *__restrict__ counts, uint32_t cluster_slots, uint32_t *__restrict__ words)
+{
+    const uint32_t c16 = counts[K_S16H], c32 = counts[K_S32H], cg = counts[K_GENH];
+    const bool clusters = (c16 + 1) / 2 + c32 + cg <= 2 * cluster_slots;
+    words[0] = clusters ? c16 : 0u;
+    words[1] = clusters ? c32 : 0u;
+    words[2] = clusters ? cg : 0u;
+    words[3] = clusters ? 0u : c16;
+    words[4] = clusters ? 0u : c32;
+    words[5] = clusters ? 0u : cg;
 }
 
 }  // namespace pa

@@ -1,5 +1,6 @@
-"""CTA mode: long pairs computed by whole thread blocks (the warps pipeline the
-pair's row passes through ring rows with published progress).
+"""CTA and cluster modes: long pairs computed by whole thread blocks (the warps
+pipeline the pair's row passes through ring rows with published progress), the
+largest by clusters of 4 blocks (flags read through distributed shared memory).
 
 Parity with the oracle for local, global and free-end global alignment, the
 byte-compare class, the s16 -> s32 redo of long pairs, the device entry point,
@@ -151,3 +152,51 @@ def test_cta_band_mode_exact(pa, oracle):
         al = pa.Aligner(dict(c, band_mode=2), context=ctx)
         res = al.compute_arrays(d["seq1"], d["off1"], d["seq2"], d["off2"])
         _check(oracle, c, d["seq1"], d["off1"], d["seq2"], d["off2"], res)
+
+
+@pytest.mark.parametrize("c", [_cfg(), _cfg(local=True, match=1, mismatch=-4, gap_open=-6),
+                               _cfg(last_row_free=True, last_column_free=True)])
+def test_cluster_forced_on_short_pairs(pa, oracle, c):
+    q, qo, t, to = _pairs(7, SHORT * 2)
+    ctx = pa.Context(0)
+    ctx.set_cta_threshold(1)
+    ctx.set_cluster_threshold(1, 1)
+    al = pa.Aligner(c, context=ctx)
+    res = al.compute_arrays(q, qo, t, to)
+    _check(oracle, c, q, qo, t, to, res)
+
+
+@pytest.mark.parametrize("c", [_cfg(), _cfg(local=True, match=1, mismatch=-4, gap_open=-6)])
+def test_cluster_mode_largest_pairs(pa, oracle, c):
+    """Pairs above the default cluster threshold (2^28 cells, 8192 rows), with smaller ones beside."""
+    q, qo, t, to = _pairs(8, [(17000, 16500), (16600, 17100), (3000, 2900), (400, 500)], div=0.06)
+    al = pa.Aligner(c)
+    res = al.compute_arrays(q, qo, t, to)
+    _check(oracle, c, q, qo, t, to, res)
+
+
+def test_cluster_band_mode_exact(pa, oracle):
+    d = workloads.config5(seed=57, n_pairs=60, strata=(0.5, 0.3, 0.2))
+    c = _cfg(match=1, mismatch=-4, gap_open=-6)
+    for w0 in (4, 64):
+        ctx = pa.Context(0)
+        ctx.set_cta_threshold(1 << 16)
+        ctx.set_cluster_threshold(1 << 20, 1024)
+        ctx.set_band_options(straight_w0=w0, w_min=2, full_frac=0.9)
+        al = pa.Aligner(dict(c, band_mode=2), context=ctx)
+        res = al.compute_arrays(d["seq1"], d["off1"], d["seq2"], d["off2"])
+        _check(oracle, c, d["seq1"], d["off1"], d["seq2"], d["off2"], res)
+
+
+def test_largest_pairs_routed_to_blocks_when_many(pa, oracle):
+    """More largest-class units than two waves of clusters: the CTA kernel takes them ahead of
+    its own list (the lead list); with few, the clusters take them.  Both must be exact."""
+    q, qo, t, to = _pairs(9, SHORT * 30)            # 420 pairs: more than 2 x resident clusters units
+    c = _cfg()
+    for cells in (1, 1 << 40):
+        ctx = pa.Context(0)
+        ctx.set_cta_threshold(1)
+        ctx.set_cluster_threshold(cells, 1)
+        al = pa.Aligner(c, context=ctx)
+        res = al.compute_arrays(q, qo, t, to)
+        _check(oracle, c, q, qo, t, to, res)
