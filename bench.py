@@ -294,12 +294,13 @@ def our_arm(args):
     # end to end through the host-buffer C ABI from pinned memory
     pin = {k: torch.from_numpy(np.ascontiguousarray(d[k])).pin_memory() for k in ("seq1", "off1", "seq2", "off2")}
     hs = {k: v.numpy() for k, v in pin.items()}
+    res_pin = torch.empty(n * 16, dtype=torch.uint8).pin_memory().numpy().view(pa.RESULT_DTYPE)
     for _ in range(2):
-        al.compute_arrays(hs["seq1"], hs["off1"], hs["seq2"], hs["off2"], stats=False)
+        al.compute_arrays(hs["seq1"], hs["off1"], hs["seq2"], hs["off2"], stats=False, out=res_pin)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        host_res = al.compute_arrays(hs["seq1"], hs["off1"], hs["seq2"], hs["off2"], stats=False)
+        host_res = al.compute_arrays(hs["seq1"], hs["off1"], hs["seq2"], hs["off2"], stats=False, out=res_pin)
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
     assert np.array_equal(host_res["score"], res["score"]), "host and device entry points disagree"
     h2d = int(sum(pin[k].numel() * pin[k].element_size() for k in pin))

@@ -102,7 +102,7 @@ typedef struct pa_options {
     int32_t blocks_per_sm;      /* persistent grid occupancy: 0 auto                       */
     int32_t use_graphs;         /* 0 auto(on), 1 on, -1 off                                */
     int32_t autotune;           /* 0 off, 1 on first use                                   */
-    int32_t kernel_variant;     /* inner-loop form: -1 auto, 0 three-operand max, 1 short chain */
+    int32_t kernel_variant;     /* inner-loop form: -1 auto (per-method tuning), else 0..6 (pa_tuning) */
     int32_t reserved[2];
 } pa_options;
 

@@ -203,8 +203,11 @@ class Aligner:
 
     # -- bulk entry points ----------------------------------------------------
     def compute_arrays(self, seq1: np.ndarray, off1: np.ndarray, seq2: np.ndarray, off2: np.ndarray,
-                       stats: bool = True) -> np.ndarray:
-        """Host arrays in, structured result array (RESULT_DTYPE) out.  Synchronous."""
+                       stats: bool = True, out: np.ndarray | None = None) -> np.ndarray:
+        """Host arrays in, structured result array (RESULT_DTYPE) out.  Synchronous.
+
+        `out` (RESULT_DTYPE, at least n_pairs long, ideally in pinned memory) receives the results
+        instead of a newly allocated array."""
         n = len(off1) - 1
         if len(off2) - 1 != n:
             raise ValueError("both sequence collections must hold the same number of sequences")
@@ -212,7 +215,10 @@ class Aligner:
         seq2 = np.ascontiguousarray(seq2, dtype=np.uint8)
         off1 = np.ascontiguousarray(off1, dtype=np.uint64)
         off2 = np.ascontiguousarray(off2, dtype=np.uint64)
-        out = np.zeros(max(n, 1), dtype=RESULT_DTYPE)
+        if out is None:
+            out = np.zeros(max(n, 1), dtype=RESULT_DTYPE)
+        elif out.dtype != RESULT_DTYPE or len(out) < n or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous RESULT_DTYPE array of at least n_pairs entries")
         st = _lib.PaStats()
         ctx = self.context
         cfg = self.c_config()

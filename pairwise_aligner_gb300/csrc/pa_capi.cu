@@ -33,6 +33,7 @@ namespace {
 constexpr int kR = 16;             // rows per thread per lane
 constexpr int64_t kDefaultRingM = 65536;   // device entry points: CTA mode up to this sequence1 length
 constexpr int kDefaultG = 8;       // threads per group
+constexpr int kVariants = 7;       // inner-loop variants (pa_kern_v*.cu)
 
 struct DevBuf {
     void *p = nullptr;
@@ -177,11 +178,15 @@ int dp_occupancy_v1(bool lanes16, bool gen, int mode);
 int dp_occupancy_v2(bool lanes16, bool gen, int mode);
 int dp_occupancy_v3(bool lanes16, bool gen, int mode);
 int dp_occupancy_v4(bool lanes16, bool gen, int mode);
+int dp_occupancy_v5(bool lanes16, bool gen, int mode);
+int dp_occupancy_v6(bool lanes16, bool gen, int mode);
 void dp_launch_v0(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v1(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v2(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v3(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v4(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
+void dp_launch_v5(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
+void dp_launch_v6(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 
 int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
 {
@@ -189,6 +194,8 @@ int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
     if (variant == 2) return dp_occupancy_v2(lanes16, gen, mode);
     if (variant == 3) return dp_occupancy_v3(lanes16, gen, mode);
     if (variant == 4) return dp_occupancy_v4(lanes16, gen, mode);
+    if (variant == 5) return dp_occupancy_v5(lanes16, gen, mode);
+    if (variant == 6) return dp_occupancy_v6(lanes16, gen, mode);
     return dp_occupancy_v0(lanes16, gen, mode);
 }
 
@@ -218,6 +225,8 @@ void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStre
     else if (variant == 2) dp_launch_v2(lanes16, gen, mode, grid, st, L, P);
     else if (variant == 3) dp_launch_v3(lanes16, gen, mode, grid, st, L, P);
     else if (variant == 4) dp_launch_v4(lanes16, gen, mode, grid, st, L, P);
+    else if (variant == 5) dp_launch_v5(lanes16, gen, mode, grid, st, L, P);
+    else if (variant == 6) dp_launch_v6(lanes16, gen, mode, grid, st, L, P);
     else dp_launch_v0(lanes16, gen, mode, grid, st, L, P);
 }
 }  // namespace pa
@@ -227,7 +236,7 @@ namespace {
 // Resident blocks per SM of every DP kernel, queried once outside any stream capture.
 void warm_occupancy()
 {
-    for (int v = 0; v < 5; ++v)
+    for (int v = 0; v < kVariants; ++v)
         for (int mode = 0; mode < 3; ++mode) {
             dp_occupancy(v, true, false, mode);
             dp_occupancy(v, false, false, mode);
@@ -948,7 +957,7 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
         c->fixed_G = true;
     }
     if (c->opt.rows_per_thread && c->opt.rows_per_thread != kR) { pa_destroy(c); return PA_ERR_UNSUPPORTED; }
-    if (c->opt.kernel_variant >= 0 && c->opt.kernel_variant <= 4) {
+    if (c->opt.kernel_variant >= 0 && c->opt.kernel_variant < kVariants) {
         for (int k = 0; k < 3; ++k) c->variant[k] = c->opt.kernel_variant;
         c->fixed_variant = true;
     }
@@ -1141,10 +1150,15 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
     const uint64_t *h1 = off1, *h2 = off2;
     if (base1) { r1.assign(off1, off1 + n_pairs + 1); for (auto &v : r1) v -= base1; h1 = r1.data(); }
     if (base2) { r2.assign(off2, off2 + n_pairs + 1); for (auto &v : r2) v -= base2; h2 = r2.data(); }
-    if (b1) PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_seq1.p, seq1 + base1, b1, cudaMemcpyHostToDevice, st));
+    // the two sequence sets go over two copy engines at once (side stream joins before the DP)
+    PA_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+    PA_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+    if (b1) PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_seq1.p, seq1 + base1, b1, cudaMemcpyHostToDevice, ctx->side));
+    PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off1.p, h1, (n_pairs + 1) * 8, cudaMemcpyHostToDevice, ctx->side));
     if (b2) PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_seq2.p, seq2 + base2, b2, cudaMemcpyHostToDevice, st));
-    PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off1.p, h1, (n_pairs + 1) * 8, cudaMemcpyHostToDevice, st));
     PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off2.p, h2, (n_pairs + 1) * 8, cudaMemcpyHostToDevice, st));
+    PA_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
+    PA_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
     if (config && config->band_mode) {
         s = run_band(ctx, config, (const uint8_t *)ctx->in_seq1.p, (const uint64_t *)ctx->in_off1.p, b1,
                      (const uint8_t *)ctx->in_seq2.p, (const uint64_t *)ctx->in_off2.p, b2, n_pairs,
@@ -1308,7 +1322,7 @@ pa_status pa_get_tuning(const pa_ctx *ctx, pa_tuning *out)
 }
 
 static bool valid_G(int g) { return g >= 1 && g <= 32 && (g & (g - 1)) == 0; }
-static bool valid_variant(int v) { return v >= 0 && v <= 4; }
+static bool valid_variant(int v) { return v >= 0 && v < kVariants; }
 
 pa_status pa_set_tuning(pa_ctx *ctx, const pa_tuning *t)
 {
@@ -1333,9 +1347,9 @@ pa_status pa_autotune(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1,
     std::vector<pa_result> res(std::max<uint64_t>(n_pairs, 1));
     double best = 1e300;
     pa_tuning choice = saved;
-    static const int kVariants[] = {0, 1, 3, 4};
+    static const int kCandidates[] = {0, 1, 3, 4, 5, 6};
     static const int kGroups[] = {4, 8, 16};
-    for (int v : kVariants)
+    for (int v : kCandidates)
         for (int g : kGroups) {
             pa_tuning t = saved;
             t.variant_s16[mi] = t.variant_s32[mi] = v;

@@ -241,6 +241,28 @@ __device__ __forceinline__ uint32_t stored(const GroupWork &w, int32_t true_valu
     return V::splat(x);
 }
 
+// Maximum of x[0..N) as a tree of three-operand maxima (depth log3 N, not N/2).
+template <class V, int N>
+__device__ __forceinline__ uint32_t tree_max(const uint32_t *x)
+{
+    if constexpr (N == 1) {
+        return x[0];
+    } else if constexpr (N == 2) {
+        return V::max2(x[0], x[1]);
+    } else if constexpr (N == 3) {
+        return V::max3(x[0], x[1], x[2]);
+    } else {
+        constexpr int M = (N + 2) / 3;
+        uint32_t y[M];
+#pragma unroll
+        for (int k = 0; k < M; ++k) {
+            const int a = 3 * k, left = N - a;
+            y[k] = left >= 3 ? V::max3(x[a], x[a + 1], x[a + 2]) : (left == 2 ? V::max2(x[a], x[a + 1]) : x[a]);
+        }
+        return tree_max<V, M>(y);
+    }
+}
+
 // VAR bit 0: short-chain form of the vertical gap; bit 2: branch-free top input for
 // thread 0 and an L1 prefetch of the score tables eight columns ahead.
 template <class V, int R, int RA, int MODE, bool GEN, int VAR, int SYNC = 0>
@@ -339,6 +361,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
         }
     }
     constexpr bool TUNED = (VAR & 4) != 0;
+    constexpr bool SPARSE = (VAR & 16) != 0;        // prefetches once per 8 columns, boundary included
     const bool first_thread = t == 0;
     const bool top_border = first_thread && p == 0;
     const bool top_buffer = first_thread && p > 0;
@@ -354,7 +377,18 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             if (top_buffer && i < iend) advance(i);
             upH = top_border ? nt : (top_buffer ? c.h : upH);
             upE = top_border ? V::subc(nt, GOEA) : (top_buffer ? c.e : upE);
-            if (!GEN && i + 8 <= iend) {
+            if (SPARSE) {
+                // one prefetch per 8 columns: the score-table line 24 columns ahead, and for
+                // thread 0 the boundary row 32 columns ahead (written by the pass above, it is
+                // in L2 but not in this SM's L1)
+                if ((i & 7) == 0) {
+                    if (!GEN && i + 24 <= iend) {
+                        asm volatile("prefetch.global.L1 [%0];" ::"l"(w.qt[0] + min(i + 24, w.m[0])));
+                        if (NL == 2) asm volatile("prefetch.global.L1 [%0];" ::"l"(w.qt[1] + min(i + 24, w.m[1])));
+                    }
+                    if (!SYNC && top_buffer && i + 32 <= iend) asm volatile("prefetch.global.L1 [%0];" ::"l"(w.bin + i + 32));
+                }
+            } else if (!GEN && i + 8 <= iend) {
                 asm volatile("prefetch.global.L1 [%0];" ::"l"(w.qt[0] + min(i + 7, w.m[0])));
                 if (NL == 2) asm volatile("prefetch.global.L1 [%0];" ::"l"(w.qt[1] + min(i + 7, w.m[1])));
             }
@@ -441,9 +475,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             }
         }
         if (MODE == M_LOCAL) {
-            uint32_t cm = H[0];
-#pragma unroll
-            for (int k = 1; k < RA; k += 2) cm = V::max3(cm, H[k], H[k + 1 < RA ? k + 1 : k]);
+            const uint32_t cm = tree_max<V, RA>(H);
             const uint32_t nb = V::max2(best, cm);
             const uint32_t x = nb ^ best;
             best = nb;

@@ -2,13 +2,19 @@
 // with PA_VARIANT defined.  Variant 0: three-operand H max, 2 blocks/SM;
 // 1: short-chain H, 2 blocks/SM; 2: as 0 with at most 85 registers (3 blocks/SM);
 // 3: as 0 with a branch-free top input and L1 prefetch of the score tables;
-// 4: as 3 with the two-op vertical-gap chain.
+// 4: as 3 with the two-op vertical-gap chain; 5 and 6: as 3 and 4 with one prefetch per
+// 8 columns that also covers the pass-boundary row.
 #ifndef PA_VARIANT
 #error "define PA_VARIANT"
 #endif
 
 namespace {
-constexpr int kVarMath = PA_VARIANT == 1 ? 1 : (PA_VARIANT == 3 ? 4 : (PA_VARIANT == 4 ? 12 : 0));
+constexpr int kVarMath = PA_VARIANT == 1   ? 1
+                         : PA_VARIANT == 3 ? 4
+                         : PA_VARIANT == 4 ? 12
+                         : PA_VARIANT == 5 ? 20
+                         : PA_VARIANT == 6 ? 28
+                                           : 0;
 constexpr int kVarMinB = PA_VARIANT == 2 ? 3 : 2;
 constexpr int kRows = 16;
 
