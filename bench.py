@@ -46,10 +46,10 @@ METRIC = "GCUPS (m*n cells/s), affine-gap local score DP + end coordinates, bit-
 METRIC_GLOBAL = "GCUPS (m*n cells/s), affine-gap global score DP, bit-exact"
 WORKLOAD = "config2_local_262144_pairs_64-512bp_+1/-4/-6/-1"
 BAND_MODEL = os.path.join(REPO, "pairwise_aligner_gb300", "data", "band_model.npz")
-# DRAM bytes per cell of the s16x2 local DP kernel, from the ncu capture summarised in
-# profiles/dp_kernel_s16x2_local_config2.md (dram__bytes_read.sum + dram__bytes_write.sum
-# of a 32,768-pair launch divided by its 2.71e9 cells; traffic grows with the cells).
-DRAM_BYTES_PER_CELL = (49.625600e6 + 3.836672e6) / 2714564472
+# DRAM bytes per cell of the s16x2 local DP kernel, from one ncu capture of its launch on the
+# first 32,768 pairs of this workload (dram__bytes_read.sum + dram__bytes_write.sum divided by
+# the launch's 2.7146e9 cells; the traffic grows with the cells).
+DRAM_BYTES_PER_CELL = (49.953280e6 + 4.400640e6) / 2714564472
 
 
 def env_rank():
