@@ -228,6 +228,8 @@ def our_arm(args):
         model = BD.BandModel(device=dev)
         model.load(BAND_MODEL)
         model.to_context(ctx)
+    if args.band and args.band_margin > 0:
+        ctx.set_band_options(margin=args.band_margin)
     al = Aligner(conf, device=local_rank, context=ctx)
     peak = ctx.roofline()
 
@@ -335,6 +337,7 @@ def our_arm(args):
     }
     if args.band:
         line["band"] = {k: st[k] for k in ("pairs_banded", "pairs_full_dp", "band_cells", "band_rounds")}
+        line["band"]["options"] = ctx.band_options()
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rate, npairs, dt = cpu_sample_rate(d, args.cpu_seconds, threads)
@@ -389,6 +392,7 @@ def main():
     ap.add_argument("--workload", choices=["config1", "config2", "config3", "config4", "config5"], default="config2")
     ap.add_argument("--band", type=int, choices=[0, 1, 2], default=0,
                     help="band mode for global workloads: 1 learned (shipped weights), 2 straight")
+    ap.add_argument("--band-margin", type=float, default=0.0, help="band mode: start-width margin (default 1.25)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

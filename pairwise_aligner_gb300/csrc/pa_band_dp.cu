@@ -68,7 +68,7 @@ __device__ __forceinline__ int32_t half_width(const BandSpec &B, int32_t i, int3
 __global__ void k_band_windows(const uint64_t *__restrict__ off1, const uint64_t *__restrict__ off2,
                                const uint32_t *__restrict__ list, uint32_t count, const BandSpec *__restrict__ spec,
                                int32_t rows, int shift, float full_frac, int2 *__restrict__ win,
-                               uint8_t *__restrict__ code)
+                               uint8_t *__restrict__ code, unsigned long long *__restrict__ width_stats)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
@@ -115,7 +115,12 @@ __global__ void k_band_windows(const uint64_t *__restrict__ off1, const uint64_t
         pa = x.x;
         pb = x.y;
     }
-    code[k] = (double)cells > (double)full_frac * (double)m * (double)n ? 2 : 0;
+    const bool full = (double)cells > (double)full_frac * (double)m * (double)n;
+    code[k] = full ? 2 : 0;
+    if (!full && width_stats) {          // mean window width of the banded pairs (team size)
+        atomicAdd(width_stats, (unsigned long long)(cells / rows));
+        atomicAdd(width_stats + 1, (unsigned long long)P);
+    }
 }
 
 // Network outputs (16 floats per pair, 9 used) -> band: checkpoint diagonals
@@ -265,7 +270,7 @@ int band_occ()
     if (per_sm < 0) {
         int v = 0;
         if (CTA)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel_cta<V, 16, M_BAND, false, kBandVar>, kBlock, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel_team<V, 16, M_BAND, false, kBandVar, 1>, kBlock, 0);
         else
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel<V, 16, M_BAND, false, kBandVar, 2>, kBlock, 0);
         per_sm = v < 1 ? 1 : v;
@@ -287,8 +292,18 @@ int band_cta_occupancy() { return std::max(band_dp_occupancy(true, true), band_d
 void band_dp_launch(bool lanes16, bool cta, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
 {
     if (cta) {
-        if (lanes16) dp_kernel_cta<L16, 16, M_BAND, false, kBandVar><<<grid, kBlock, 0, st>>>(L, P);
-        else dp_kernel_cta<L32, 16, M_BAND, false, kBandVar><<<grid, kBlock, 0, st>>>(L, P);
+        // teams of L.team warps per pair (narrow bands keep few passes in flight)
+        if (lanes16) {
+            if (L.team == 1) dp_kernel_team<L16, 16, M_BAND, false, kBandVar, 1><<<grid, kBlock, 0, st>>>(L, P);
+            else if (L.team == 2) dp_kernel_team<L16, 16, M_BAND, false, kBandVar, 2><<<grid, kBlock, 0, st>>>(L, P);
+            else if (L.team == 4) dp_kernel_team<L16, 16, M_BAND, false, kBandVar, 4><<<grid, kBlock, 0, st>>>(L, P);
+            else dp_kernel_cta<L16, 16, M_BAND, false, kBandVar><<<grid, kBlock, 0, st>>>(L, P);
+        } else {
+            if (L.team == 1) dp_kernel_team<L32, 16, M_BAND, false, kBandVar, 1><<<grid, kBlock, 0, st>>>(L, P);
+            else if (L.team == 2) dp_kernel_team<L32, 16, M_BAND, false, kBandVar, 2><<<grid, kBlock, 0, st>>>(L, P);
+            else if (L.team == 4) dp_kernel_team<L32, 16, M_BAND, false, kBandVar, 4><<<grid, kBlock, 0, st>>>(L, P);
+            else dp_kernel_cta<L32, 16, M_BAND, false, kBandVar><<<grid, kBlock, 0, st>>>(L, P);
+        }
     } else if (lanes16) {
         dp_kernel<L16, 16, M_BAND, false, kBandVar, 2><<<grid, kBlock, 0, st>>>(L, P);
     } else {
@@ -296,12 +311,14 @@ void band_dp_launch(bool lanes16, bool cta, int grid, cudaStream_t st, const DpL
     }
 }
 
+// width_stats (2 device words, may be null) accumulates the window widths and passes of
+// the pairs that stay banded.
 void band_windows_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, const uint32_t *list,
                          uint32_t count, const BandSpec *spec, int32_t rows, int shift, float full_frac, int2 *win,
-                         uint8_t *code)
+                         uint8_t *code, unsigned long long *width_stats)
 {
     if (count) k_band_windows<<<blocks(count, 128), 128, 0, st>>>(off1, off2, list, count, spec, rows, shift,
-                                                                   full_frac, win, code);
+                                                                   full_frac, win, code, width_stats);
 }
 
 void band_decode_launch(cudaStream_t st, const float *out, const uint64_t *off1, const uint64_t *off2,

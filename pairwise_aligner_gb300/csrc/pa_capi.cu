@@ -208,7 +208,7 @@ int band_cta_occupancy();
 void band_dp_launch(bool lanes16, bool cta, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
 void band_windows_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, const uint32_t *list,
                          uint32_t count, const BandSpec *spec, int32_t rows, int shift, float full_frac, int2 *win,
-                         uint8_t *code);
+                         uint8_t *code, unsigned long long *width_stats);
 void band_decode_launch(cudaStream_t st, const float *out, const uint64_t *off1, const uint64_t *off2,
                         uint64_t n_pairs, const DpParams &P, float margin, int32_t w_min, BandSpec *spec);
 void band_straight_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, uint64_t n_pairs,
@@ -577,6 +577,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         F.count_ptr = count_word;
         F.unit_counter = queue;
         F.rerun = 0;
+        F.team = 0;                                   // whole blocks per pair
         F.rerun_list = (uint32_t *)(bc[k].kind ? c->rerun_long.p : c->rerun.p);
         F.rerun_count = counters + (bc[k].kind ? 6 : 4);
         if (bc[k].kind == 2) {
@@ -653,16 +654,23 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     auto band_step = [&](int k, const uint32_t *list, uint32_t count, int r, bool rerun, uint32_t *next,
                          uint32_t &n_next, uint32_t *redo_out, uint32_t &n_redo) -> pa_status {
         const BandClass &B = bc[k];
-        band_windows_launch(st, o1, o2, list, count, spec, B.rows, r, full_frac, (int2 *)c->band_win.p, code);
+        unsigned long long *wstat = (unsigned long long *)(ctr + 36);
+        PA_CUDA(c, cudaMemsetAsync(wstat, 0, 16, st));
+        band_windows_launch(st, o1, o2, list, count, spec, B.rows, r, full_frac, (int2 *)c->band_win.p, code, wstat);
         compact_launch(st, list, code, count, 2, bsum, full[k] + nfull[k], ctr + 1);
         compact_launch(st, list, code, count, 0, bsum, tmp, ctr + 2);
         c->last_launches += 7;
         uint32_t h[2];
+        unsigned long long ws[2];
         PA_CUDA(c, cudaMemcpyAsync(h, ctr + 1, 8, cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaMemcpyAsync(ws, wstat, 16, cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaStreamSynchronize(st));
         nfull[k] += h[0];
         const uint32_t nb = h[1];
         if (nb == 0) return PA_OK;
+        // CTA mode: a team of warps per pair sized to the passes a window keeps in flight
+        const double mean_width = ws[1] ? (double)ws[0] / (double)ws[1] : 0.0;
+        L.team = mean_width >= 8.0 * B.rows ? 8 : mean_width >= 4.0 * B.rows ? 4 : mean_width >= 2.0 * B.rows ? 2 : 1;
         PA_CUDA(c, cudaMemsetAsync(ctr + 3, 0, 4, st));
         L.order = tmp;
         L.begin_ptr = ctr + 0;
@@ -714,6 +722,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
             ncur[k] = nn[k];
         }
     }
+    L.team = 0;                                       // the full DP below: whole blocks per pair
     // still open after the last round: full DP
     uint32_t hc[NB];
     for (int k = 0; k < NB; ++k) {

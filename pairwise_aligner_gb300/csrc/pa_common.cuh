@@ -88,6 +88,7 @@ struct DpLaunch {
     // CTA mode (long pairs): each block owns ring rows of ring_stride cells, one per group
     Cell *ring;
     uint64_t ring_stride;
+    int32_t team;                 // band mode, CTA launches: warps per unit (1, 2, 4 or 8; 0 means 8)
     uint32_t *error;              // error bits (kErrWaitTimeout), may be null
 };
 

@@ -928,6 +928,110 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cta(DpLaunch L, DpParams 
     }
 }
 
+// Teams mode (band mode on long pairs): the warps of a block form teams of T warps
+// (1, 2, 4 or 8); each team takes one unit (one pair, two in s16x2 lanes) at a time and its warps
+// take the unit's passes round robin: pass p runs on team warp p % T, reads the boundary
+// row of pass p - 1 from that warp's ring row and writes its own, column by column, behind
+// published progress.  A team's ring row k is reused by pass p + T only after pass p + 1
+// has read it: pass p + T reaches column c only after every pass between did.  Teams
+// smaller than the block suit banded pairs, whose narrow windows keep only a few passes in
+// flight at once.
+template <class V, int R, int MODE, bool GEN, int VAR, int T>
+__global__ void __launch_bounds__(kBlock, 2) dp_kernel_team(DpLaunch L, DpParams P)
+{
+    static_assert(R % kChunk == 0 && R <= 32, "R must be a multiple of the chunk");
+    constexpr int NL = V::LANES;
+    constexpr int NW = kBlock / 32;
+    constexpr int G = 32;
+    __shared__ uint4 snap_store[MODE == M_LOCAL ? NL * (R / 4) * kBlock : 1];
+    __shared__ int prog[NW];
+    __shared__ uint32_t s_unit[NW];
+    __shared__ int32_t s_cand[NW][2][4];
+    __shared__ int32_t s_lb[MODE == M_LABEL_REV ? NW : 1][8][2];
+    __shared__ unsigned long long s_cells[NW];
+    // the unit lists, in shared memory so that they hold no registers during the passes
+    __shared__ const uint32_t *s_order[2];
+    __shared__ uint32_t s_count[2], s_units_lead, s_units;
+    if (threadIdx.x == 0) {
+        const uint32_t cm = *L.count_ptr, cl = L.lead_count_ptr ? *L.lead_count_ptr : 0u;
+        s_order[0] = L.order + *L.begin_ptr;
+        s_order[1] = L.lead_count_ptr ? L.lead_order + *L.lead_begin_ptr : nullptr;
+        s_count[0] = cm;
+        s_count[1] = cl;
+        s_units_lead = (cl + NL - 1) / NL;
+        s_units = s_units_lead + (cm + NL - 1) / NL;
+    }
+    __syncthreads();
+    static_assert(T == 1 || T == 2 || T == 4 || T == kBlock / 32, "team of 1, 2, 4 or all warps");
+    const int t = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const unsigned gmask = 0xffffffffu;
+    auto team_sync = [&]() {
+        if (T == 1) __syncwarp();
+        else asm volatile("bar.sync %0, %1;" ::"r"(1 + g / T), "r"(T * 32) : "memory");
+    };
+
+    for (;;) {
+        if (t == 0) prog[g] = -1;
+        if (g % T == 0 && t == 0) s_unit[g / T] = atomicAdd(L.unit_counter, 1u);
+        team_sync();
+        uint32_t u = s_unit[g / T];
+        team_sync();
+        const uint32_t units_lead = *(volatile uint32_t *)&s_units_lead, n_units = *(volatile uint32_t *)&s_units;
+        if (u >= n_units) break;
+        // the lead list first, then the main list, each largest shapes first
+        const int which = u < units_lead ? 1 : 0;
+        u = which ? units_lead - 1 - u : n_units - 1 - u;
+        const uint32_t first = u * NL;
+        GroupWork w;
+        init_work<V, MODE>(L, P, *(const uint32_t *volatile *)&s_order[which], first,
+                           *(volatile uint32_t *)&s_count[which], G, R, w);
+        const int32_t span = w.ms + 2;           // progress values of consecutive passes never overlap
+        for (int p = g % T; p < w.passes; p += T) {
+            const int lead = g - g % T, pw = (p + T - 1) % T;   // team's first warp; warp of pass p - 1
+            Cell *ring = L.ring + ((uint64_t)blockIdx.x * NW + lead) * L.ring_stride;
+            w.bin = ring + (uint64_t)pw * L.ring_stride;
+            w.bout = ring + (uint64_t)(p % T) * L.ring_stride;
+            w.prog_in = &prog[lead + pw];
+            w.prog_out = &prog[g];
+            w.base_in = (p - 1) * span;
+            w.base_out = p * span;
+            w.seen = INT32_MIN;
+            pass_body<V, R, MODE, GEN, VAR, 1>(L, P, w, p, t, G, gmask, snap_store);
+            if (t == G - 1 && p + 1 < w.passes) publish_progress<1>(w.prog_out, w.base_out + w.ms + 1);
+        }
+        reduce_group<V, MODE>(w, gmask, G);
+        if (t == 0) {
+            for (int l = 0; l < 2; ++l) {
+                s_cand[g][l][0] = w.cs[l];
+                s_cand[g][l][1] = w.ci[l];
+                s_cand[g][l][2] = w.cj[l];
+                s_cand[g][l][3] = w.ub[l];
+            }
+            if (MODE == M_LABEL_REV)
+                for (int c = 0; c < 8; ++c) { s_lb[g][c][0] = w.lb_v[c]; s_lb[g][c][1] = w.lb_j[c]; }
+            s_cells[g] = w.cells;
+        }
+        team_sync();
+        if (g % T == 0 && t == 0) {
+            for (int k = g + 1; k < g + T; ++k) {
+                for (int l = 0; l < 2; ++l) {
+                    const int32_t *c = s_cand[k][l];
+                    if (better(c[0], c[1], c[2], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = c[0]; w.ci[l] = c[1]; w.cj[l] = c[2]; }
+                    w.ub[l] = max(w.ub[l], c[3]);
+                }
+                if (MODE == M_LABEL_REV)
+                    for (int c = 0; c < 8; ++c) {
+                        const int32_t ov = s_lb[k][c][0], oj = s_lb[k][c][1];
+                        if (ov > w.lb_v[c] || (ov == w.lb_v[c] && oj < w.lb_j[c])) { w.lb_v[c] = ov; w.lb_j[c] = oj; }
+                    }
+                w.cells += s_cells[k];
+            }
+            emit<V, MODE>(L, P, w, first);
+        }
+        team_sync();
+    }
+}
+
 // Cluster mode for the largest pairs: a cluster of CL blocks (co-scheduled by the
 // hardware) works on one unit with all its 8*CL warps, pass p on group p % (8*CL)
 // (block (p % (8*CL)) / 8, warp p % 8).  Progress flags stay in the shared memory

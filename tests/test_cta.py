@@ -200,3 +200,15 @@ def test_largest_pairs_routed_to_blocks_when_many(pa, oracle):
         al = pa.Aligner(c, context=ctx)
         res = al.compute_arrays(q, qo, t, to)
         _check(oracle, c, q, qo, t, to, res)
+
+
+def test_band_teams_of_warps_exact(pa, oracle):
+    """Narrow bands on long pairs run with teams of 1-4 warps per pair inside a block."""
+    q, qo, t, to = _pairs(10, [(6000, 6100), (5000, 4900), (7000, 7050), (4500, 4600)] * 3, div=0.03)
+    c = _cfg(match=1, mismatch=-4, gap_open=-6)
+    for w0 in (16, 200, 700, 1500):
+        ctx = pa.Context(0)
+        ctx.set_band_options(straight_w0=w0, w_min=8, full_frac=0.9)
+        al = pa.Aligner(dict(c, band_mode=2), context=ctx)
+        res = al.compute_arrays(q, qo, t, to)
+        _check(oracle, c, q, qo, t, to, res)
