@@ -318,8 +318,17 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
     // inside a capture the record must become a graph node to fire on every replay
     const unsigned ev_flags = capturing == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
     PA_CUDA(c, cudaEventRecordWithFlags(c->ev_dp0, st, ev_flags));
-    // the largest pairs first, on the side stream: clusters of blocks per pair; the kernels
-    // below fill the SMs those clusters leave free
+    // s16x2 class
+    L.begin_ptr = ranges + K_S16; L.count_ptr = counts + K_S16; L.unit_counter = counters + 0; L.G = c->G[K_S16];
+    launch_class(c, K_S16, mode, true, false, L, P);
+    // s32 class
+    L.begin_ptr = ranges + K_S32; L.count_ptr = counts + K_S32; L.unit_counter = counters + 1; L.G = c->G[K_S32];
+    launch_class(c, K_S32, mode, false, false, L, P);
+    // byte-compare class
+    L.begin_ptr = ranges + K_GEN; L.count_ptr = counts + K_GEN; L.unit_counter = counters + 2; L.G = c->G[K_GEN];
+    launch_class(c, K_GEN, mode, false, true, L, P);
+    // the largest pairs, on the side stream forked after the group kernels: clusters of blocks
+    // per pair, beside the CTA-mode kernels below, which fill the SMs the clusters leave free
     DpLaunch LL = L;
     if (c->ring.p) {
         LL.ring = (Cell *)c->ring.p;
@@ -340,15 +349,6 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
         }
         PA_CUDA(c, cudaEventRecord(c->ev_join, c->side));
     }
-    // s16x2 class
-    L.begin_ptr = ranges + K_S16; L.count_ptr = counts + K_S16; L.unit_counter = counters + 0; L.G = c->G[K_S16];
-    launch_class(c, K_S16, mode, true, false, L, P);
-    // s32 class
-    L.begin_ptr = ranges + K_S32; L.count_ptr = counts + K_S32; L.unit_counter = counters + 1; L.G = c->G[K_S32];
-    launch_class(c, K_S32, mode, false, false, L, P);
-    // byte-compare class
-    L.begin_ptr = ranges + K_GEN; L.count_ptr = counts + K_GEN; L.unit_counter = counters + 2; L.G = c->G[K_GEN];
-    launch_class(c, K_GEN, mode, false, true, L, P);
     // long pairs: whole blocks per pair; their s16 results that fail the check are redone in s32
     if (c->ring.p) {
         const Klass lc[3] = {K_S16L, K_S32L, K_GENL}, hl[3] = {K_S16H, K_S32H, K_GENH};
