@@ -50,6 +50,10 @@ typedef enum pa_status {
 
 typedef enum pa_method { PA_METHOD_GLOBAL = 0, PA_METHOD_LOCAL = 1 } pa_method;
 
+/* Added to pa_config.method: score with the context's substitution matrix
+ * (pa_set_substitution_matrix; cfg::score_model_matrix) instead of match/mismatch. */
+#define PA_SCORE_MATRIX 0x100
+
 /* Alignment configuration.  Replaces the compile-time rule chain
  * cfg::method_global / cfg::method_local (method_global.hpp:121-145,
  * method_local.hpp:118-137), cfg::gap_model_affine (gap_model_affine.hpp:130-155)
@@ -223,6 +227,14 @@ pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells);
  * computed by clusters of 4 thread blocks (co-scheduled; their 32 warps pipeline the
  * pair's passes); defaults 2^28 and 8192. */
 pa_status pa_set_cluster_threshold(pa_ctx *ctx, uint64_t cells, uint32_t min_rows);
+
+/* Substitution-matrix scoring (configuration/score_model_matrix.hpp:203-222,
+ * score_model/score_model_matrix.hpp:53-63): symbols[r] is the symbol of rank r,
+ * scores[r1 * dim + r2] the score of a sequence1 symbol of rank r1 against a
+ * sequence2 symbol of rank r2 (dim <= 32, |score| <= 2^20).  Calls whose config has
+ * PA_SCORE_MATRIX use it; every symbol of their sequences must be in `symbols`
+ * (else PA_ERR_INVALID_ARGUMENT).  Not with band mode. */
+pa_status pa_set_substitution_matrix(pa_ctx *ctx, const uint8_t *symbols, uint32_t dim, const int32_t *scores);
 
 /* Band mode (no counterpart in the reference, which has no banded mode).
  * A pair's band: the centre line through (0, 0), the checkpoints

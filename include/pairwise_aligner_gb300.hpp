@@ -20,6 +20,9 @@
 // reference's only runtime error does (tracker_global_simd_saturated.hpp:98-100).
 #pragma once
 
+#include <array>
+#include <concepts>
+#include <cstddef>
 #include <cstdint>
 #include <memory>
 #include <ranges>
@@ -57,6 +60,8 @@ struct settings {
     int32_t gap_open = 0, gap_extension = 0;
     int32_t match = 0, mismatch = 0;
     int32_t width_hint = 0;
+    std::vector<uint8_t> matrix_symbols;     // score_model_matrix: symbol of each rank
+    std::vector<int32_t> matrix_scores;      // ... and the flat dim x dim scores
 };
 
 struct initial_t {
@@ -154,6 +159,34 @@ inline constexpr score_model_unitary_fn score_model_unitary{};
 inline constexpr score_model_unitary_fn score_model_unitary_simd{};
 inline constexpr score_model_unitary_fn score_model_unitary_simd_saturated{};
 
+// cfg::score_model_matrix(pred, matrix) (configuration/score_model_matrix.hpp:203-222): the
+// same argument type as the reference, an array of (symbol, row of scores) pairs; the score
+// of sequence1 symbol a against sequence2 symbol b is row(a)[rank(b)].
+inline constexpr struct score_model_matrix_fn {
+    template <configuration_rule pred_t, typename alphabet_t, std::integral score_t, size_t dim>
+    auto operator()(pred_t pred, std::array<std::pair<alphabet_t, std::array<score_t, dim>>, dim> const &m) const
+    {
+        static_assert(dim >= 1 && dim <= 32, "the GB300 kernels take up to 32 symbols");
+        std::array<uint8_t, dim> sym{};
+        std::array<int32_t, dim * dim> sc{};
+        for (size_t r = 0; r < dim; ++r) {
+            sym[r] = static_cast<uint8_t>(m[r].first);
+            for (size_t k = 0; k < dim; ++k) sc[r * dim + k] = static_cast<int32_t>(m[r].second[k]);
+        }
+        return make_rule(std::move(pred), [sym, sc](settings &s) {
+            if (s.has_score) throw std::runtime_error("configuration has more than one score model");
+            s.has_score = true;
+            s.matrix_symbols.assign(sym.begin(), sym.end());
+            s.matrix_scores.assign(sc.begin(), sc.end());
+        });
+    }
+    template <typename alphabet_t, std::integral score_t, size_t dim>
+    auto operator()(std::array<std::pair<alphabet_t, std::array<score_t, dim>>, dim> const &m) const
+    {
+        return (*this)(initial, m);
+    }
+} score_model_matrix{};
+
 }  // namespace cfg
 
 // One result: score(), the two sequences, and the 1-based end position.
@@ -195,6 +228,12 @@ public:
         pa_ctx *c = nullptr;
         check(pa_create(&c, device, nullptr), nullptr);
         _ctx = std::shared_ptr<pa_ctx>(c, [](pa_ctx *p) { pa_destroy(p); });
+        if (!s.matrix_symbols.empty()) {
+            _cfg.method |= PA_SCORE_MATRIX;
+            check(pa_set_substitution_matrix(_ctx.get(), s.matrix_symbols.data(),
+                                             static_cast<uint32_t>(s.matrix_symbols.size()), s.matrix_scores.data()),
+                  _ctx.get());
+        }
     }
 
     // Bulk: ranges of character sequences, same length; any number of pairs.

@@ -34,6 +34,9 @@ class OracleCfg(ctypes.Structure):
         ("first_row_free", ctypes.c_int32),
         ("last_column_free", ctypes.c_int32),
         ("last_row_free", ctypes.c_int32),
+        ("dim", ctypes.c_int32),
+        ("matrix", ctypes.POINTER(ctypes.c_int32)),
+        ("rank", ctypes.POINTER(ctypes.c_int16)),
     ]
 
 
@@ -74,10 +77,23 @@ def lib():
 
 
 def make_cfg(match, mismatch, gap_open, gap_extension, local=False, first_column_free=False,
-             first_row_free=False, last_column_free=False, last_row_free=False) -> OracleCfg:
-    return OracleCfg(int(match), int(mismatch), int(gap_open), int(gap_extension), int(bool(local)),
-                     int(bool(first_column_free)), int(bool(first_row_free)), int(bool(last_column_free)),
-                     int(bool(last_row_free)))
+             first_row_free=False, last_column_free=False, last_row_free=False, matrix=None) -> OracleCfg:
+    """`matrix`: optional substitution matrix as (symbols, dim x dim scores) -- row = sequence1 symbol."""
+    cfg = OracleCfg(int(match), int(mismatch), int(gap_open), int(gap_extension), int(bool(local)),
+                    int(bool(first_column_free)), int(bool(first_row_free)), int(bool(last_column_free)),
+                    int(bool(last_row_free)), 0, None, None)
+    if matrix is not None:
+        symbols, scores = matrix
+        dim = len(symbols)
+        rank = np.full(256, -1, dtype=np.int16)
+        for r, sym in enumerate(symbols):
+            rank[sym if isinstance(sym, int) else ord(sym)] = r
+        mat = np.ascontiguousarray(np.asarray(scores, dtype=np.int32).reshape(dim, dim))
+        cfg.dim = dim
+        cfg.matrix = _ptr(mat, ctypes.c_int32)
+        cfg.rank = _ptr(rank, ctypes.c_int16)
+        cfg._keep = (mat, rank)                     # the arrays live as long as the config
+    return cfg
 
 
 def _ptr(a, t):

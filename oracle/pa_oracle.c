@@ -16,6 +16,9 @@
  *       - border cells: include/pairwise_aligner/affine/affine_initialisation_strategy.hpp:38-51
  *       - local clamp of the diagonal term: include/pairwise_aligner/matrix/dp_matrix_local.hpp:39-47
  *       - substitution: include/pairwise_aligner/score_model/score_model_unitary.hpp:52-59
+ *         or, with a matrix, include/pairwise_aligner/score_model/score_model_matrix.hpp:53-63
+ *         (score = matrix[rank(sequence1 symbol) * dim + rank(sequence2 symbol)], the
+ *         ranks from the symbol list as in configuration/score_model_matrix.hpp:203-222)
  *       - global result (+ free trailing row/column): include/pairwise_aligner/tracker/tracker_global_scalar.hpp:36-61
  *       - local result (max over all cells, lowest() when empty): include/pairwise_aligner/tracker/tracker_local_scalar.hpp:38-49
  *     Parity is pinned against the reference's hand-written golden scores
@@ -56,7 +59,26 @@ typedef struct pa_oracle_cfg {
     int32_t first_row_free;     /* leading gap in sequence2 free (H(0,j) = 0) */
     int32_t last_column_free;   /* result may end in column n            */
     int32_t last_row_free;      /* result may end in row m               */
+    int32_t dim;                /* substitution matrix: 0 = unitary scores */
+    const int32_t *matrix;      /* dim x dim, row = sequence1 symbol       */
+    const int16_t *rank;        /* 256 entries: symbol -> rank, -1 invalid */
 } pa_oracle_cfg;
+
+static inline int64_t substitute(const pa_oracle_cfg *c, uint8_t a, uint8_t b)
+{
+    if (c->dim) return c->matrix[c->rank[a] * c->dim + c->rank[b]];
+    return a == b ? c->match : c->mismatch;
+}
+
+/* With a matrix every symbol must have a rank (the reference asserts it). */
+static int symbols_valid(const pa_oracle_cfg *c, const uint8_t *s, uint64_t len)
+{
+    if (!c->dim) return 1;
+    if (!c->matrix || !c->rank || c->dim < 0) return 0;
+    for (uint64_t k = 0; k < len; ++k)
+        if (c->rank[s[k]] < 0 || c->rank[s[k]] >= c->dim) return 0;
+    return 1;
+}
 
 static inline int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
 
@@ -81,6 +103,7 @@ int pa_oracle_align(const pa_oracle_cfg *c, const uint8_t *s1, uint64_t m, const
                     int64_t *score, int64_t *end1, int64_t *end2)
 {
     if (!c || !score || !end1 || !end2) return PA_ORACLE_EINVAL;
+    if (!symbols_valid(c, s1, m) || !symbols_valid(c, s2, n)) return PA_ORACLE_EINVAL;
     const int local = c->local != 0;
     const int first_col_free = local || c->first_column_free;
     const int first_row_free = local || c->first_row_free;
@@ -117,7 +140,7 @@ int pa_oracle_align(const pa_oracle_cfg *c, const uint8_t *s1, uint64_t m, const
         hrow[0] = hc;
         const uint8_t a = s1[i - 1];
         for (uint64_t j = 1; j <= n; ++j) {
-            int64_t d = diag + ((a == s2[j - 1]) ? c->match : c->mismatch);
+            int64_t d = diag + substitute(c, a, s2[j - 1]);
             if (local) d = max64(d, 0);                       /* dp_matrix_local.hpp:39-47 */
             int64_t h = max64(max64(d, vgap[j]), hgap);
             diag = hrow[j];
@@ -165,6 +188,7 @@ int pa_oracle_row(const pa_oracle_cfg *c, const uint8_t *s1, uint64_t m, const u
                   uint64_t row, int64_t *out)
 {
     if (!c || !out || row > m || c->local) return PA_ORACLE_EINVAL;
+    if (!symbols_valid(c, s1, m) || !symbols_valid(c, s2, n)) return PA_ORACLE_EINVAL;
     const int64_t goe = (int64_t)c->gap_open + c->gap_extension, ext = c->gap_extension;
     int64_t *vgap = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
     if (!vgap) return PA_ORACLE_ENOMEM;
@@ -175,7 +199,7 @@ int pa_oracle_row(const pa_oracle_cfg *c, const uint8_t *s1, uint64_t m, const u
         int64_t diag = out[0];
         out[0] = hc;
         for (uint64_t j = 1; j <= n; ++j) {
-            int64_t h = max64(max64(diag + ((s1[i - 1] == s2[j - 1]) ? c->match : c->mismatch), vgap[j]), hgap);
+            int64_t h = max64(max64(diag + substitute(c, s1[i - 1], s2[j - 1]), vgap[j]), hgap);
             diag = out[j];
             out[j] = h;
             int64_t hoe = h + goe;
@@ -394,6 +418,7 @@ int pa_oracle_simd_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint64
 {
     if (!c || !scores || (n_pairs && (!off1 || !off2))) return PA_ORACLE_EINVAL;
     if (c->local == 0 && (c->last_column_free || c->last_row_free)) return PA_ORACLE_EINVAL;
+    if (c->dim) return PA_ORACLE_EINVAL;                /* the SIMD port scores unitary only */
     uint32_t *order = (uint32_t *)malloc(sizeof(uint32_t) * (n_pairs ? n_pairs : 1));
     if (!order) return PA_ORACLE_ENOMEM;
     uint64_t n_simd = 0;

@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(_HERE, "libpa_gb300.so")
 
 PA_METHOD_GLOBAL = 0
 PA_METHOD_LOCAL = 1
+PA_SCORE_MATRIX = 0x100      # or-ed into PaConfig.method: score with the context's substitution matrix
 
 STATUS = {
     0: "PA_OK", 1: "PA_ERR_INVALID_ARGUMENT", 2: "PA_ERR_CUDA", 3: "PA_ERR_OUT_OF_MEMORY",
@@ -152,6 +153,7 @@ SIGNATURES = {
     "pa_set_band_options": ([_ctxp, ctypes.POINTER(PaBandOptions)], ctypes.c_int),
     "pa_get_band_options": ([_ctxp, ctypes.POINTER(PaBandOptions)], ctypes.c_int),
     "pa_set_band_model": ([_ctxp] + [ctypes.c_void_p] * 6, ctypes.c_int),
+    "pa_set_substitution_matrix": ([_ctxp, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
     "pa_align_batch_banded": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.POINTER(PaStats)], ctypes.c_int),

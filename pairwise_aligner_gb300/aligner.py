@@ -69,6 +69,18 @@ class Context:
         """Of the block-mode pairs, those with at least `cells` cells and `min_rows` rows run on clusters."""
         _lib.check(self.lib.pa_set_cluster_threshold(self.ptr, int(cells), int(min_rows)), self.ptr)
 
+    def set_substitution_matrix(self, symbols: bytes, scores):
+        """Load the matrix that PA_SCORE_MATRIX calls score with: scores[r1 * dim + r2] for a
+        sequence1 symbol of rank r1 (its index in `symbols`) against a sequence2 symbol of rank r2."""
+        sym = np.frombuffer(bytes(symbols), dtype=np.uint8).copy()
+        sc = np.ascontiguousarray(np.asarray(scores, dtype=np.int64).reshape(-1))
+        if sc.size != sym.size * sym.size or np.abs(sc).max(initial=0) > (1 << 20):
+            raise ValueError("scores must hold dim * dim values in [-2^20, 2^20]")
+        sc = sc.astype(np.int32)
+        _lib.check(self.lib.pa_set_substitution_matrix(self.ptr, sym.ctypes.data, int(sym.size), sc.ctypes.data),
+                   self.ptr)
+        self._matrix = (bytes(symbols), tuple(int(x) for x in sc))
+
     # -- band mode ----------------------------------------------------------------
     def band_options(self) -> dict:
         o = _lib.PaBandOptions()
@@ -187,12 +199,18 @@ class Aligner:
     def context(self) -> Context:
         if self._ctx is None:
             self._ctx = Context(self.device)
+        mat = self.config.get("matrix")
+        if mat is not None and getattr(self._ctx, "_matrix", None) != mat:
+            self._ctx.set_substitution_matrix(*mat)       # a context holds one matrix at a time
         return self._ctx
 
     def c_config(self) -> _lib.PaConfig:
         c = self.config
+        method = _lib.PA_METHOD_LOCAL if c["local"] else _lib.PA_METHOD_GLOBAL
+        if c.get("matrix") is not None:
+            method |= _lib.PA_SCORE_MATRIX
         return _lib.PaConfig(
-            _lib.PA_METHOD_LOCAL if c["local"] else _lib.PA_METHOD_GLOBAL, c["match"], c["mismatch"],
+            method, c["match"], c["mismatch"],
             c["gap_open"], c["gap_extension"], int(c["first_column_free"]), int(c["first_row_free"]),
             int(c["last_column_free"]), int(c["last_row_free"]), int(c.get("width_hint", 0)),
             int(c.get("band_mode", 0)))

@@ -127,6 +127,33 @@ score_model_unitary_simd = score_model_unitary_gpu
 score_model_unitary_simd_saturated = score_model_unitary_gpu
 
 
+def score_model_matrix(*args):
+    """cfg::score_model_matrix(pred, matrix) (configuration/score_model_matrix.hpp:203-222).
+
+    ``matrix`` is a sequence of ``(symbol, row)`` pairs, as the reference's
+    ``std::array<std::pair<alphabet_t, std::array<score_t, D>>, D>``: the score of a
+    sequence1 symbol ``s1`` against a sequence2 symbol ``s2`` is ``row(s1)[rank(s2)]``,
+    where the rank of a symbol is its position in the list (score_model/
+    score_model_matrix.hpp:53-63).  Up to 32 symbols (single bytes or 1-character
+    strings); every symbol of the aligned sequences must be one of them."""
+    pred, (matrix,) = _split(args, 1, "score_model_matrix")
+    symbols, rows = [], []
+    for sym, row in matrix:
+        b = sym.encode() if isinstance(sym, str) else (bytes([sym]) if isinstance(sym, int) else bytes(sym))
+        if len(b) != 1:
+            raise TypeError("score_model_matrix: every symbol must be one byte")
+        symbols.append(b[0])
+        rows.append([int(x) for x in row])
+    dim = len(symbols)
+    if not 1 <= dim <= 32 or any(len(r) != dim for r in rows):
+        raise ValueError("score_model_matrix: a square matrix of 1..32 symbols is required")
+    if len(set(symbols)) != dim:
+        raise ValueError("score_model_matrix: symbols must be distinct")
+    flat = tuple(x for r in rows for x in r)
+    return _Rule(rule_category.score_model, {"match": 0, "mismatch": 0,
+                                             "matrix": (bytes(symbols), flat)}, pred)
+
+
 def band_learned(*args):
     """Opt-in learned band for global alignment: banded DP checked by an admissible
     bound, doubling to the full DP when the bound does not certify the band."""

@@ -82,6 +82,9 @@ struct pa_ctx {
     DevBuf band_list[20];
     DevBuf mlp_w[6], mlp_feat, mlp_x, mlp_h1, mlp_h2, mlp_out;
     bool has_model = false;
+    // substitution matrix (PA_SCORE_MATRIX): int8 rank per byte (-1: not a symbol), int32 scores
+    DevBuf mat_rank, mat_scores;
+    int32_t mat_dim = 0, mat_max = 0, mat_min = 0;
 };
 
 namespace {
@@ -128,18 +131,27 @@ pa_status ensure(pa_ctx *c, DevBuf &b, size_t bytes)
 pa_status check_config(pa_ctx *c, const pa_config *cfg, DpParams &P, ClassCfg &C)
 {
     if (!cfg) return fail(c, PA_ERR_INVALID_ARGUMENT, "config is null");
-    if (cfg->method != PA_METHOD_GLOBAL && cfg->method != PA_METHOD_LOCAL)
-        return fail(c, PA_ERR_INVALID_ARGUMENT, "method must be PA_METHOD_GLOBAL or PA_METHOD_LOCAL");
+    const int32_t method = cfg->method & ~PA_SCORE_MATRIX;
+    const bool use_matrix = (cfg->method & PA_SCORE_MATRIX) != 0;
+    if (method != PA_METHOD_GLOBAL && method != PA_METHOD_LOCAL)
+        return fail(c, PA_ERR_INVALID_ARGUMENT,
+                    "method must be PA_METHOD_GLOBAL or PA_METHOD_LOCAL (optionally | PA_SCORE_MATRIX)");
+    if (use_matrix && (!c || c->mat_dim == 0))
+        return fail(c, PA_ERR_INVALID_ARGUMENT, "PA_SCORE_MATRIX needs pa_set_substitution_matrix first");
+    if (use_matrix && cfg->band_mode != 0)
+        return fail(c, PA_ERR_UNSUPPORTED, "band mode scores with match/mismatch only");
     if (cfg->gap_extension > 0 || (int64_t)cfg->gap_open + cfg->gap_extension > 0)
         return fail(c, PA_ERR_UNSUPPORTED, "positive gap scores are not supported");
     if (cfg->width_hint != 0 && cfg->width_hint != 16 && cfg->width_hint != 32)
         return fail(c, PA_ERR_INVALID_ARGUMENT, "width_hint must be 0, 16 or 32");
     if (cfg->band_mode < 0 || cfg->band_mode > 2)
         return fail(c, PA_ERR_INVALID_ARGUMENT, "band_mode must be 0, 1 or 2");
-    const bool local = cfg->method == PA_METHOD_LOCAL;
+    const bool local = method == PA_METHOD_LOCAL;
     std::memset(&P, 0, sizeof(P));
-    P.match = cfg->match;
-    P.mismatch = cfg->mismatch;
+    // with a matrix, match / mismatch hold its largest and smallest score: the bounds that
+    // the padding score, the column shift and the overflow check need
+    P.match = use_matrix ? c->mat_max : cfg->match;
+    P.mismatch = use_matrix ? c->mat_min : cfg->mismatch;
     P.gap_open = cfg->gap_open;
     P.gap_ext = cfg->gap_extension;
     P.local = local;
@@ -147,13 +159,15 @@ pa_status check_config(pa_ctx *c, const pa_config *cfg, DpParams &P, ClassCfg &C
     P.first_row_free = local || cfg->first_row_free;
     P.last_column_free = !local && cfg->last_column_free;
     P.last_row_free = !local && cfg->last_row_free;
-    P.smax = std::max(0, std::max(cfg->match, cfg->mismatch));
-    P.spad = std::min(0, std::min(cfg->match, cfg->mismatch));
+    P.smax = std::max(0, std::max(P.match, P.mismatch));
+    P.spad = std::min(0, std::min(P.match, P.mismatch));
     P.shift = local ? 0 : P.smax;
     P.floor16 = -32768 + 1280;
     std::memset(&C, 0, sizeof(C));
-    C.fast_scores = cfg->match >= -127 && cfg->match <= 127 && cfg->mismatch >= -127 && cfg->mismatch <= 0 &&
-                    cfg->match - P.shift >= -128 && cfg->mismatch - P.shift >= -128;   // byte tables of shifted scores
+    C.fast_scores = !use_matrix && cfg->match >= -127 && cfg->match <= 127 && cfg->mismatch >= -127 &&
+                    cfg->mismatch <= 0 && cfg->match - P.shift >= -128 &&
+                    cfg->mismatch - P.shift >= -128;   // byte tables of shifted scores
+    C.rank_map = use_matrix ? (const int8_t *)c->mat_rank.p : nullptr;
     C.s16_params = (int64_t)cfg->gap_open + cfg->gap_extension >= -1000 && cfg->gap_extension >= -1000;
     C.force32 = cfg->width_hint == 32;
     C.local = local;
@@ -309,6 +323,11 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
     L.boundary = (Cell *)c->boundary.p;
     L.rerun_list = (uint32_t *)c->rerun.p;
     L.rerun_count = counters + 4;
+    if (C.rank_map) {
+        L.rank_map = C.rank_map;
+        L.matrix = (const int32_t *)c->mat_scores.p;
+        L.mdim = c->mat_dim;
+    }
     (void)b1;
 
     const uint32_t *ranges = (const uint32_t *)c->ranges.p;
@@ -437,7 +456,7 @@ pa_status prepare_buffers(pa_ctx *c, uint64_t n_pairs, uint64_t b1)
 void apply_tuning(pa_ctx *c, const pa_config *cfg)
 {
     if (!cfg) return;
-    const int mi = cfg->method == PA_METHOD_LOCAL ? 0 : 1;
+    const int mi = (cfg->method & ~PA_SCORE_MATRIX) == PA_METHOD_LOCAL ? 0 : 1;
     if (!c->fixed_variant) {
         c->variant[K_S16] = c->tuning.variant_s16[mi];
         c->variant[K_S32] = c->variant[K_GEN] = c->tuning.variant_s32[mi];
@@ -800,6 +819,7 @@ pa_status read_stats(pa_ctx *c, pa_stats *stats)
     }
     if (ctr[8]) return fail(c, PA_ERR_TIMEOUT, "a CTA-mode progress wait ran out");
     if (ps.overflow) return fail(c, PA_ERR_OVERFLOW, "scores of some pairs could exceed int32");
+    if (ps.invalid) return fail(c, PA_ERR_INVALID_ARGUMENT, "a sequence holds a symbol outside the substitution matrix");
     return PA_OK;
 }
 
@@ -986,7 +1006,8 @@ pa_status pa_destroy(pa_ctx *c)
                       &c->counts, &c->qtab, &c->boundary, &c->rerun, &c->counters, &c->pstats,
                       &c->in_seq1, &c->in_off1, &c->in_seq2, &c->in_off2, &c->in_out,
                       &c->band_spec, &c->band_win, &c->band_code, &c->band_bsum, &c->band_ctr, &c->band_in,
-                      &c->mlp_feat, &c->mlp_x, &c->mlp_h1, &c->mlp_h2, &c->mlp_out};
+                      &c->mlp_feat, &c->mlp_x, &c->mlp_h1, &c->mlp_h2, &c->mlp_out,
+                      &c->ring, &c->rerun_long, &c->mat_rank, &c->mat_scores};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     for (DevBuf &b : c->band_list)
@@ -1070,6 +1091,43 @@ pa_status pa_set_cluster_threshold(pa_ctx *ctx, uint64_t cells, uint32_t min_row
     ctx->huge_cells = cells > (uint64_t)INT64_MAX ? INT64_MAX : (int64_t)std::max<uint64_t>(cells, 1);
     ctx->huge_min_n = (int32_t)std::min<uint32_t>(std::max<uint32_t>(min_rows, 1), 1u << 30);
     for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    ctx->graphs.clear();
+    return PA_OK;
+}
+
+// The reference keeps the matrix as one flat array indexed by rank(sequence1 symbol) * dim +
+// rank(sequence2 symbol) (score_model/score_model_matrix.hpp:53-63; the ranks come from its
+// alphabet conversion, configuration/score_model_matrix.hpp:203-222).  Here the rank map is
+// a byte -> int8 table, so any byte alphabet of up to 32 symbols works.
+pa_status pa_set_substitution_matrix(pa_ctx *ctx, const uint8_t *symbols, uint32_t dim, const int32_t *scores)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    if (!symbols || !scores) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null matrix");
+    if (dim < 1 || dim > 32) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "matrix dim must be 1..32");
+    int8_t rank[256];
+    std::memset(rank, -1, sizeof(rank));
+    for (uint32_t r = 0; r < dim; ++r) {
+        if (rank[symbols[r]] >= 0) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "matrix symbols must be distinct");
+        rank[symbols[r]] = (int8_t)r;
+    }
+    int32_t hi = INT32_MIN, lo = INT32_MAX;
+    for (uint32_t k = 0; k < dim * dim; ++k) {
+        if (scores[k] > (1 << 20) || scores[k] < -(1 << 20))
+            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "matrix scores must lie in [-2^20, 2^20]");
+        hi = std::max(hi, scores[k]);
+        lo = std::min(lo, scores[k]);
+    }
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, PA_ERR_CUDA, "cudaSetDevice");
+    PA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));      // no call in flight reads the old matrix
+    PA_CUDA(ctx, cudaStreamSynchronize(ctx->side));
+    pa_status s;
+    if ((s = ensure(ctx, ctx->mat_rank, 256)) || (s = ensure(ctx, ctx->mat_scores, 32 * 32 * 4))) return s;
+    PA_CUDA(ctx, cudaMemcpy(ctx->mat_rank.p, rank, 256, cudaMemcpyHostToDevice));
+    PA_CUDA(ctx, cudaMemcpy(ctx->mat_scores.p, scores, (size_t)dim * dim * 4, cudaMemcpyHostToDevice));
+    ctx->mat_dim = (int32_t)dim;
+    ctx->mat_max = hi;
+    ctx->mat_min = lo;
+    for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);   // they hold the old dim
     ctx->graphs.clear();
     return PA_OK;
 }
@@ -1339,7 +1397,7 @@ pa_status pa_set_tuning(pa_ctx *ctx, const pa_tuning *t)
     for (int m = 0; m < 2; ++m)
         if (!valid_variant(t->variant_s16[m]) || !valid_variant(t->variant_s32[m]) || !valid_G(t->group_threads_s16[m]) ||
             !valid_G(t->group_threads_s32[m]))
-            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "tuning: variant must be 0..4 and group_threads 1..32, power of two");
+            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "tuning: variant must be 0..6 and group_threads 1..32, power of two");
     ctx->tuning = *t;
     ctx->fixed_G = ctx->fixed_variant = false;
     return PA_OK;
@@ -1349,7 +1407,7 @@ pa_status pa_autotune(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1,
                       const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, pa_tuning *out)
 {
     if (!ctx || !config) return PA_ERR_INVALID_ARGUMENT;
-    const int mi = config->method == PA_METHOD_LOCAL ? 0 : 1;
+    const int mi = (config->method & ~PA_SCORE_MATRIX) == PA_METHOD_LOCAL ? 0 : 1;
     const pa_tuning saved = ctx->tuning;
     const bool fg = ctx->fixed_G, fv = ctx->fixed_variant;
     ctx->fixed_G = ctx->fixed_variant = false;

@@ -90,6 +90,11 @@ struct DpLaunch {
     uint64_t ring_stride;
     int32_t team;                 // band mode, CTA launches: warps per unit (1, 2, 4 or 8; 0 means 8)
     uint32_t *error;              // error bits (kErrWaitTimeout), may be null
+    // substitution-matrix scoring (byte-compare kernels): symbol -> rank (-1 invalid) and the
+    // dim x dim scores, row = sequence1 rank; null for the unitary model
+    const int8_t *rank_map;
+    const int32_t *matrix;
+    int32_t mdim;
 };
 
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)

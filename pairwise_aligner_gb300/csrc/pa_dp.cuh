@@ -288,6 +288,12 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
     const bool left_out = BAND && ibase > 0;        // column ibase lies outside the band
     const uint32_t NEGV = V::LANES == 2 ? CLAMP : (uint32_t)kNeg32;
 
+    // byte-compare kernels with a substitution matrix: held rows carry the symbol's rank,
+    // streamed columns rank * dim (both below 0x400 for dim <= 32); 0x400 / 0x800 mark
+    // padding (and an invalid symbol, which the classifier reports as an error)
+    const bool MAT = GEN && L.matrix != nullptr;
+    auto rank_of = [&](uint8_t b) -> int { return (int)__ldg(L.rank_map + b); };
+
     uint32_t H[RA], Fr[RA], Sel[RA];
 #pragma unroll
     for (int k = 0; k < RA; ++k) {
@@ -295,8 +301,15 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
         int c[2];
 #pragma unroll
         for (int l = 0; l < 2; ++l) {
-            if (GEN) c[l] = (j < w.n[l]) ? (int)L.seq2[w.toff[l] + j] : 0x100;
-            else c[l] = (j < w.n[l]) ? (int)dna_code(L.seq2[w.toff[l] + j]) : -1;
+            if (GEN) {
+                c[l] = (j < w.n[l]) ? (int)L.seq2[w.toff[l] + j] : 0x100;
+                if (MAT) {
+                    const int r = c[l] < 0x100 ? rank_of((uint8_t)c[l]) : -1;
+                    c[l] = r < 0 ? 0x400 : r;
+                }
+            } else {
+                c[l] = (j < w.n[l]) ? (int)dna_code(L.seq2[w.toff[l] + j]) : -1;
+            }
         }
         Sel[k] = GEN ? (uint32_t)c[0] : V::selector(c[0], c[1]);
         H[k] = left_out ? NEGV : stored<V>(w, border(P, P.first_row_free, (int64_t)j + 1));
@@ -325,6 +338,10 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
     auto load_tables = [&](int32_t col, uint32_t &a, uint32_t &b) {
         if (GEN) {
             a = (col <= w.m[0]) ? (uint32_t)L.seq1[w.qoff[0] + col - 1] : 0x200u;
+            if (MAT) {
+                const int r = a < 0x200u ? rank_of((uint8_t)a) : -1;
+                a = r < 0 ? 0x800u : (uint32_t)(r * L.mdim);
+            }
             b = a;
         } else {
             a = __ldg(w.qt[0] + min(col - 1, w.m[0]));
@@ -412,8 +429,11 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
             uint32_t sc;
             if (GEN) {
                 const uint32_t x = Sel[k];
-                sc = (x == ta) ? (uint32_t)(P.match - P.shift)
-                               : (((x | ta) >> 8) ? (uint32_t)(P.spad - P.shift) : (uint32_t)(P.mismatch - P.shift));
+                if (MAT)
+                    sc = ((x | ta) >> 10) ? (uint32_t)(P.spad - P.shift) : (uint32_t)(__ldg(L.matrix + ta + x) - P.shift);
+                else
+                    sc = (x == ta) ? (uint32_t)(P.match - P.shift)
+                                   : (((x | ta) >> 8) ? (uint32_t)(P.spad - P.shift) : (uint32_t)(P.mismatch - P.shift));
             } else {
                 sc = prmt(ta, tb, Sel[k]);
             }

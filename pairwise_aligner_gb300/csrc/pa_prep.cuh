@@ -21,12 +21,14 @@ struct ClassCfg {
     int64_t huge_cells;      // ... and with m*n at least this and n >= huge_min_n to cluster mode
     int32_t long_max_m;      // the longest sequence1 the ring rows hold
     int32_t huge_min_n;
+    const int8_t *rank_map;  // substitution-matrix scoring: symbol -> rank (null: unitary scores)
 };
 
 struct PrepStats {
     unsigned long long cells;
     unsigned long long n_class[16];
     unsigned long long overflow;    // pairs whose int32 bound fails
+    unsigned long long invalid;     // substitution-matrix scoring: pairs with a symbol outside it
 };
 
 __device__ __forceinline__ uint32_t quant_len(uint32_t m)
@@ -97,6 +99,13 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
             if (left > 3) dna &= dna_valid(q[3]);
         }
         dna = __all_sync(0xffffffffu, dna);
+        if (C.rank_map) {                                 // every symbol needs a rank
+            bool ok = true;
+            for (int64_t j = lane; j < n; j += 32) ok &= C.rank_map[seq2[t0 + j]] >= 0;
+            for (int64_t i = lane; i < m; i += 32) ok &= C.rank_map[seq1[q0 + i]] >= 0;
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok && lane == 0) atomicAdd(&st->invalid, 1ull);
+        }
         uint32_t klass;
         if (m == 0 || n == 0) klass = K_NONE;
         else if (!C.fast_scores || !dna) klass = K_GEN;

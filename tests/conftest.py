@@ -25,6 +25,25 @@ def kats():
 
 
 @pytest.fixture(scope="session")
+def matrix_kats():
+    """The reference's substitution-matrix known answers and their matrices."""
+    with open(os.path.join(GOLDEN, "kat_matrix.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
+def matrix_cases():
+    """The reference's substitution-matrix SIMD differential cases with oracle results."""
+    with gzip.open(os.path.join(GOLDEN, "matrix_differential.json.gz"), "rt") as f:
+        return json.load(f)
+
+
+def matrix_of(m: dict):
+    """(symbols bytes, flat dim*dim scores) of a golden-fixture matrix."""
+    return "".join(m["symbols"]).encode(), [x for row in m["scores"] for x in row]
+
+
+@pytest.fixture(scope="session")
 def simd_cases():
     with gzip.open(os.path.join(GOLDEN, "simd_differential.json.gz"), "rt") as f:
         return json.load(f)
@@ -43,15 +62,17 @@ def built_lib():
     return build.build()
 
 
-def oracle_cfg_of(O, c: dict):
-    """Oracle configuration from a golden-fixture case."""
+def oracle_cfg_of(O, c: dict, matrix=None):
+    """Oracle configuration from a golden-fixture case (`matrix`: (symbols, scores) or None)."""
     return O.make_cfg(c["match"], c["mismatch"], c["gap_open"], c["gap_extension"], local=c["method"] == "local",
                       first_column_free=c["first_column"] == "free", first_row_free=c["first_row"] == "free",
-                      last_column_free=c["last_column"] == "free", last_row_free=c["last_row"] == "free")
+                      last_column_free=c["last_column"] == "free", last_row_free=c["last_row"] == "free",
+                      matrix=matrix)
 
 
-def rule_of(c: dict):
-    """The cfg rule chain of a golden-fixture case, written like the reference's tests."""
+def rule_of(c: dict, matrix_pairs=None):
+    """The cfg rule chain of a golden-fixture case, written like the reference's tests
+    (`matrix_pairs`: the (symbol, row) list of cfg.score_model_matrix, or None)."""
     from pairwise_aligner_gb300 import cfg
     if c["method"] == "local":
         base = cfg.method_local(cfg.gap_model_affine(c["gap_open"], c["gap_extension"]))
@@ -62,4 +83,6 @@ def rule_of(c: dict):
         trail = cfg.trailing_end_gap(last_column=e.free if c["last_column"] == "free" else e.penalised,
                                      last_row=e.free if c["last_row"] == "free" else e.penalised)
         base = cfg.method_global(cfg.gap_model_affine(c["gap_open"], c["gap_extension"]), lead, trail)
+    if matrix_pairs is not None:
+        return cfg.score_model_matrix(base, matrix_pairs)
     return cfg.score_model_unitary_gpu(base, c["match"], c["mismatch"])

@@ -6,7 +6,9 @@
 // length in [min, max] and for the symbol index into "ACGT".  This program
 // reproduces those draws with the same standard-library engine and
 // distributions so that tests/golden/ holds exactly the pairs the reference's
-// own tests align.  Usage: gen_reference_sequences SEED COUNT MIN MAX
+// own tests align.  The substitution-matrix tests draw from the matrix's symbol
+// list instead (matrix_model::symbol_list, same file :62-77).
+// Usage: gen_reference_sequences SEED COUNT MIN MAX [SYMBOLS]   (default ACGT)
 // Output: COUNT lines of sequence 1, then COUNT lines of sequence 2.
 #include <cstdio>
 #include <cstdlib>
@@ -16,19 +18,20 @@
 
 int main(int argc, char **argv)
 {
-    if (argc != 5) {
-        std::fprintf(stderr, "usage: %s SEED COUNT MIN MAX\n", argv[0]);
+    if (argc != 5 && argc != 6) {
+        std::fprintf(stderr, "usage: %s SEED COUNT MIN MAX [SYMBOLS]\n", argv[0]);
         return 2;
     }
     unsigned seed = static_cast<unsigned>(std::strtoul(argv[1], nullptr, 10));
     std::size_t count = std::strtoull(argv[2], nullptr, 10);
     std::size_t lo = std::strtoull(argv[3], nullptr, 10);
     std::size_t hi = std::strtoull(argv[4], nullptr, 10);
-    const char symbols[] = "ACGT";
+    const std::string symbols = argc == 6 ? argv[5] : "ACGT";
+    if (symbols.empty()) return 2;
 
     std::mt19937 engine{seed};
     std::uniform_int_distribution<std::size_t> length_dist{lo, hi};
-    std::uniform_int_distribution<std::size_t> symbol_dist{0, 3};
+    std::uniform_int_distribution<std::size_t> symbol_dist{0, symbols.size() - 1};
 
     std::vector<std::string> out(2 * count);
     for (std::string &s : out) {

@@ -7,12 +7,21 @@ fixtures it writes are committed, so nothing on a GPU host reads the reference.
 * kat_scalar.json -- every unitary-score case of the reference's scalar tests
   (test/unit/affine/*_scalar_test.cpp, test/unit/configuration/*.cpp): the
   configuration, both sequences and the hand-written expected score.
+* kat_matrix.json -- the substitution matrices of
+  include/pairwise_aligner/score_model/substitution_matrix.hpp (BLOSUM62 over the
+  standard and the extended amino-acid alphabets) and every matrix-score case of
+  the reference's scalar tests (test/unit/affine/*scalar*test.cpp), with their
+  hand-written expected scores.
 * simd_differential.json.gz -- every unitary-score case of the reference's SIMD
   tests (test/unit/affine/*_simd_test.cpp).  The reference checks each SIMD
   lane against its scalar aligner on std::mt19937(42) sequences; the sequences
   are regenerated with gen_reference_sequences.cpp (same engine and
   distributions) and the expected scores, plus end coordinates, come from the
   oracle's scalar restatement (oracle/pa_oracle.c), itself pinned by the KATs.
+* matrix_differential.json.gz -- the same for the reference's substitution-matrix
+  SIMD tests (test/unit/affine/*_simd_matrix_*_test.cpp): BLOSUM62, sequences drawn
+  from the matrix's symbol list, one-vs-many cases aligning the first sequence 1
+  against every sequence 2.
 
 Usage: python tests/golden/make_golden.py [--reference /root/reference]
 """
@@ -150,6 +159,43 @@ def parse_scalar_kats(ref: str) -> list[dict]:
     return cases
 
 
+def parse_substitution_matrices(ref: str) -> dict:
+    """{name: {"symbols": [...], "scores": dim x dim}} from substitution_matrix.hpp."""
+    src = open(os.path.join(ref, "include/pairwise_aligner/score_model/substitution_matrix.hpp")).read()
+    out = {}
+    for m in re.finditer(r"(blosum62_\w+)\s*\{\{(.*?)\}\};", src, re.S):
+        rows = re.findall(r"\{'(.)',\s*\{([^}]*)\}\}", m.group(2))
+        symbols = [r[0] for r in rows]
+        scores = [[int(v) for v in r[1].split(",")] for r in rows]
+        if any(len(r) != len(symbols) for r in scores):
+            raise ValueError(f"{m.group(1)}: matrix is not square")
+        out[m.group(1)] = {"symbols": symbols, "scores": scores}
+    return out
+
+
+def parse_matrix_kats(ref: str) -> list[dict]:
+    cases = []
+    d = os.path.join(ref, "test/unit/affine")
+    for fn in sorted(os.listdir(d)):
+        if not (fn.endswith("_scalar_test.cpp") or fn.endswith("_scalar_matrix_test.cpp")):
+            continue
+        rel = f"test/unit/affine/{fn}"
+        src = open(os.path.join(d, fn)).read()
+        base = _parse_base_config(src, rel)
+        for name, body, line in _blocks(src):
+            conf = re.search(r"\.configurator\s*=\s*(.*?),\s*\n\s*\.sequence1", body, re.S).group(1)
+            mm = re.search(r"score_model_matrix\(\s*base_config\s*,\s*aligner::(blosum62_\w+)<\w*>\s*\)", conf)
+            if not mm:
+                continue
+            s1 = re.search(r'\.sequence1\s*=\s*"([^"]*)"sv', body).group(1)
+            s2 = re.search(r'\.sequence2\s*=\s*"([^"]*)"sv', body).group(1)
+            exp = re.search(r"\.expected_score\s*=\s*([^\n,]+)", body).group(1).strip()
+            expected = -2**31 if "lowest()" in exp else int(exp)
+            cases.append(dict(base, matrix=mm.group(1), match=0, mismatch=0, name=name, source=f"{rel}:{line}",
+                              seq1=s1, seq2=s2, expected_score=expected))
+    return cases
+
+
 def parse_simd_cases(ref: str) -> list[dict]:
     cases = []
     d = os.path.join(ref, "test/unit/affine")
@@ -177,11 +223,43 @@ def parse_simd_cases(ref: str) -> list[dict]:
     return cases
 
 
-def oracle_cfg(c: dict):
+def parse_matrix_simd_cases(ref: str) -> list[dict]:
+    cases = []
+    d = os.path.join(ref, "test/unit/affine")
+    for fn in sorted(os.listdir(d)):
+        if not (fn.endswith("_test.cpp") and "_simd_matrix_" in fn):
+            continue
+        rel = f"test/unit/affine/{fn}"
+        src = open(os.path.join(d, fn)).read()
+        base = _parse_base_config(src, rel)
+        count_const = re.search(r"sequence_count\s*=\s*aligner::simd_score<(\w+)>::size_v", src)
+        for name, body, line in _blocks(src):
+            mm = re.search(r"matrix_model\{aligner::(blosum62_\w+)<(\w+)>\}", body)
+            if not mm:
+                continue
+            gp = re.search(r"sequence_generation_param\{\s*([^,]+),\s*(\d+),\s*(\d+)\s*\}", body)
+            cexpr = gp.group(1).strip()
+            if cexpr == "sequence_count":
+                count = LANES[count_const.group(1)]
+            else:
+                count = LANES[re.search(r"simd_score<(\w+)>", cexpr).group(1)]
+            one_vs_many = re.search(r"one_vs_many\s*=\s*std::true_type", body) is not None
+            cases.append(dict(base, match=0, mismatch=0, matrix=mm.group(1), score_type=mm.group(2),
+                              name=f"{fn[:-9]}:{name}", source=f"{rel}:{line}", seed=42, count=count,
+                              min_size=int(gp.group(2)), max_size=int(gp.group(3)), one_vs_many=one_vs_many))
+    return cases
+
+
+def oracle_cfg(c: dict, matrices: dict | None = None):
     from oracle import oracle as O
+    mat = None
+    if c.get("matrix"):
+        m = matrices[c["matrix"]]
+        mat = (m["symbols"], m["scores"])
     return O.make_cfg(c["match"], c["mismatch"], c["gap_open"], c["gap_extension"], local=c["method"] == "local",
                       first_column_free=c["first_column"] == "free", first_row_free=c["first_row"] == "free",
-                      last_column_free=c["last_column"] == "free", last_row_free=c["last_row"] == "free")
+                      last_column_free=c["last_column"] == "free", last_row_free=c["last_row"] == "free",
+                      matrix=mat)
 
 
 def main() -> int:
@@ -199,6 +277,19 @@ def main() -> int:
         json.dump(kats, f, indent=1)
     print(f"kat_scalar.json: {len(kats)} cases, oracle agrees with all")
 
+    matrices = parse_substitution_matrices(args.reference)
+    mkats = parse_matrix_kats(args.reference)
+    for k in mkats:
+        if not k["seq1"] or not k["seq2"]:
+            if k["method"] == "local" and k["expected_score"] == -2**31:
+                continue                 # the empty-sequence rule; the oracle returns it for any model
+        sc, _, _ = O.align(oracle_cfg(k, matrices), k["seq1"].encode(), k["seq2"].encode())
+        if sc != k["expected_score"]:
+            raise SystemExit(f"oracle disagrees with {k['source']} {k['name']}: {sc} != {k['expected_score']}")
+    with open(os.path.join(HERE, "kat_matrix.json"), "w") as f:
+        json.dump({"matrices": matrices, "cases": mkats}, f, indent=1)
+    print(f"kat_matrix.json: {len(matrices)} matrices, {len(mkats)} cases, oracle agrees with all")
+
     with tempfile.TemporaryDirectory() as td:
         exe = os.path.join(td, "gen")
         subprocess.check_call(["g++", "-O2", "-std=c++17", os.path.join(HERE, "gen_reference_sequences.cpp"),
@@ -213,9 +304,25 @@ def main() -> int:
             c["oracle_scores"] = [r[0] for r in res]
             c["oracle_end1"] = [r[1] for r in res]
             c["oracle_end2"] = [r[2] for r in res]
+        mcases = parse_matrix_simd_cases(args.reference)
+        for c in mcases:
+            symbols = "".join(matrices[c["matrix"]]["symbols"])
+            out = subprocess.check_output([exe, str(c["seed"]), str(c["count"]), str(c["min_size"]),
+                                           str(c["max_size"]), symbols]).decode().split("\n")
+            s1, s2 = out[:c["count"]], out[c["count"]:2 * c["count"]]
+            if c["one_vs_many"]:
+                s1 = [s1[0]] * len(s2)          # sequence1() is the first of collection 1
+            c["seqs1"], c["seqs2"] = s1, s2
+            res = [O.align(oracle_cfg(c, matrices), a.encode(), b.encode()) for a, b in zip(s1, s2)]
+            c["oracle_scores"] = [r[0] for r in res]
+            c["oracle_end1"] = [r[1] for r in res]
+            c["oracle_end2"] = [r[2] for r in res]
     with gzip.open(os.path.join(HERE, "simd_differential.json.gz"), "wt") as f:
         json.dump(cases, f)
     print(f"simd_differential.json.gz: {len(cases)} cases, {sum(c['count'] for c in cases)} pairs")
+    with gzip.open(os.path.join(HERE, "matrix_differential.json.gz"), "wt") as f:
+        json.dump(mcases, f)
+    print(f"matrix_differential.json.gz: {len(mcases)} cases, {sum(c['count'] for c in mcases)} pairs")
     return 0
 
 

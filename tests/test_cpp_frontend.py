@@ -34,6 +34,28 @@ def _line(c):
                      e("last_row"), c["seq1"] or "-", c["seq2"] or "-"])
 
 
+def _matrix_line(c, m):
+    e = lambda k: "1" if c[k] == "free" else "0"
+    scores = " ".join(str(x) for row in m["scores"] for x in row)
+    return " ".join(["M", "1" if c["method"] == "local" else "0", str(c["gap_open"]), str(c["gap_extension"]),
+                     e("first_column"), e("first_row"), e("last_column"), e("last_row"), str(len(m["symbols"])),
+                     "".join(m["symbols"]), scores, c["seq1"] or "-", c["seq2"] or "-"])
+
+
+@pytest.mark.gpu
+def test_cpp_frontend_matrix_kats(runner, matrix_kats):
+    """cfg::score_model_matrix with the reference's argument type, BLOSUM62 known answers."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    cases = matrix_kats["cases"]
+    lines = [_matrix_line(c, matrix_kats["matrices"][c["matrix"]]) for c in cases]
+    out = subprocess.run([runner], input="\n".join(lines) + "\n", capture_output=True, text=True,
+                         check=True).stdout.split("\n")
+    for c, line in zip(cases, out):
+        assert int(line.split()[0]) == c["expected_score"], (c["source"], c["name"], line)
+
+
 @pytest.mark.gpu
 def test_cpp_frontend_reference_kats(runner, kats):
     import torch

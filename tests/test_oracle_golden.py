@@ -13,7 +13,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import oracle_cfg_of
+from conftest import matrix_of, oracle_cfg_of
 
 
 def test_scalar_kats(oracle, kats):
@@ -21,6 +21,44 @@ def test_scalar_kats(oracle, kats):
     for c in kats:
         sc, e1, e2 = oracle.align(oracle_cfg_of(oracle, c), c["seq1"].encode(), c["seq2"].encode())
         assert sc == c["expected_score"], (c["source"], c["name"])
+
+
+def test_matrix_kats(oracle, matrix_kats):
+    """BLOSUM62 global / local expected scores of the reference's matrix tests."""
+    assert len(matrix_kats["cases"]) >= 6
+    for c in matrix_kats["cases"]:
+        cfg = oracle_cfg_of(oracle, c, matrix_of(matrix_kats["matrices"][c["matrix"]]))
+        sc, _, _ = oracle.align(cfg, c["seq1"].encode(), c["seq2"].encode())
+        assert sc == c["expected_score"], (c["source"], c["name"])
+
+
+def test_matrix_fixture_scores_are_the_oracles(oracle, matrix_kats, matrix_cases):
+    assert len(matrix_cases) >= 40
+    for c in matrix_cases[::5]:
+        cfg = oracle_cfg_of(oracle, c, matrix_of(matrix_kats["matrices"][c["matrix"]]))
+        for a, b, s, e1, e2 in list(zip(c["seqs1"], c["seqs2"], c["oracle_scores"], c["oracle_end1"],
+                                        c["oracle_end2"]))[:6]:
+            assert oracle.align(cfg, a.encode(), b.encode()) == (s, e1, e2)
+
+
+def test_matrix_rejects_unknown_symbol(oracle, matrix_kats):
+    cfg = oracle_cfg_of(oracle, matrix_kats["cases"][0], matrix_of(matrix_kats["matrices"]["blosum62_standard"]))
+    with pytest.raises(RuntimeError):
+        oracle.align(cfg, b"ACDJ", b"ACD")
+
+
+def test_matrix_with_unitary_scores_is_unitary(oracle):
+    """A matrix with match on the diagonal and mismatch elsewhere scores as the unitary model."""
+    rng = np.random.default_rng(3)
+    sym = b"ACGT"
+    scores = [2 if i == j else -3 for i in range(4) for j in range(4)]
+    for local in (False, True):
+        cu = oracle.make_cfg(2, -3, -5, -1, local=local)
+        cm = oracle.make_cfg(0, 0, -5, -1, local=local, matrix=(sym, scores))
+        for _ in range(20):
+            a = rng.choice(np.frombuffer(sym, np.uint8), rng.integers(0, 40)).tobytes()
+            b = rng.choice(np.frombuffer(sym, np.uint8), rng.integers(0, 40)).tobytes()
+            assert oracle.align(cu, a, b) == oracle.align(cm, a, b)
 
 
 def test_fixture_scores_are_the_oracles(oracle, simd_cases):
