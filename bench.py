@@ -12,6 +12,9 @@ One step = one call of the hot path over the whole batch:
             tables exceed the 129 MB L2, so no flush is needed between steps);
   e2e    -- the same batch through pa_align_batch with pinned HOST buffers:
             host->device copies, the DP and the device->host result read per step.
+  e2e_packed -- the same through pa_align_batch_packed: 2-bit packed host streams
+            (a quarter of the sequence bytes cross to the device; DNA workloads).
+  input_path -- GB/s of the 2-bit pack / unpack and rank-map kernels on 1 GiB.
   roofline -- the DP kernels' own duration (events inside the library) against
             the measured whole-chip rate of the cell-update instruction mix
             (pa_measure_roofline); HBM traffic against MEASURED_PEAKS.json.
@@ -308,6 +311,28 @@ def our_arm(args):
     h2d = int(sum(pin[k].numel() * pin[k].element_size() for k in pin))
     d2h = n * 16
 
+    # the same through the 2-bit packed host entry (DNA workloads; the inputs are kept packed
+    # on the host, so the packing happens before the timed region)
+    e2e_packed = None
+    acgt = np.frombuffer(b"ACGT", dtype=np.uint8)
+    if np.isin(d["seq1"], acgt).all() and np.isin(d["seq2"], acgt).all():
+        from pairwise_aligner_gb300 import seqio
+        w1 = torch.from_numpy(seqio.pack_2bit(d["seq1"])[0]).pin_memory().numpy()
+        w2 = torch.from_numpy(seqio.pack_2bit(d["seq2"])[0]).pin_memory().numpy()
+        for _ in range(2):
+            al.compute_packed(w1, hs["off1"], w2, hs["off2"], stats=False, out=res_pin)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            packed_res = al.compute_packed(w1, hs["off1"], w2, hs["off2"], stats=False, out=res_pin)
+        pk_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+        assert np.array_equal(packed_res["score"], res["score"]), "packed and byte entry points disagree"
+        e2e_packed = {"value": round(replica_throughput(cells, pk_s * 1e3, world), 2), "unit": "GCUPS",
+                      "h2d_bytes_per_step": int(w1.nbytes + w2.nbytes + pin["off1"].numel() * 8 +
+                                                pin["off2"].numel() * 8),
+                      "d2h_bytes_per_step": d2h, "entry": "pa_align_batch_packed (2-bit host streams)"}
+    input_path = input_kernels(dev, stream, ctx) if not args.no_input else None
+
     achieved = cells / (dp_ms * 1e-3) / 1e9
     peak_gcups = peak["s16x2_cells_per_s"] / 1e9
     alg_bytes = int(d["off1"][-1] + d["off2"][-1]) + 16 * n          # inputs read + results written
@@ -335,6 +360,10 @@ def our_arm(args):
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
     }
+    if e2e_packed:
+        line["e2e_packed"] = e2e_packed
+    if input_path:
+        line["input_path"] = input_path
     if args.band:
         line["band"] = {k: st[k] for k in ("pairs_banded", "pairs_full_dp", "band_cells", "band_rounds")}
         line["band"]["options"] = ctx.band_options()
@@ -348,6 +377,43 @@ def our_arm(args):
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def input_kernels(dev, stream, ctx, n: int = 1 << 30, reps: int = 5) -> dict:
+    """GB/s of the input-path kernels on 1 GiB of bytes (inputs and outputs well beyond L2):
+    algorithmic bytes = bytes read + bytes written once."""
+    import torch
+    from pairwise_aligner_gb300 import seqio
+    g = torch.Generator(device=dev).manual_seed(5)
+    codes = torch.randint(0, 4, (n,), device=dev, dtype=torch.uint8, generator=g)
+    letters = torch.tensor(list(b"ACGT"), dtype=torch.uint8, device=dev)[codes.long()]
+    del codes
+    words = torch.empty((n + 15) // 16, dtype=torch.int32, device=dev)
+    back = torch.empty(n, dtype=torch.uint8, device=dev)
+    ranks = torch.empty(n, dtype=torch.int8, device=dev)
+    out = {}
+    jobs = {"pack_2bit": (lambda: seqio.pack_2bit_device(ctx, letters, words), n + n // 4),
+            "unpack_2bit": (lambda: seqio.unpack_2bit_device(ctx, words, 0, n, back), n // 4 + n),
+            "rank_map": (lambda: seqio.rank_map_device(ctx, b"ACGTN", letters, ranks), 2 * n)}
+    peak = hbm_peak()
+    with torch.cuda.stream(stream):
+        for name, (fn, nbytes) in jobs.items():
+            fn()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+            b.synchronize()
+            ms = a.elapsed_time(b) / reps
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            out[name] = {"ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    torch.cuda.synchronize()
+    assert torch.equal(back, letters), "unpack(pack(x)) != x"
+    out.update({"bytes": n, "peak_gbs": peak, "unit": "GB/s (algorithmic bytes read + written)"})
+    del letters, words, back, ranks
+    torch.cuda.empty_cache()
+    return out
 
 
 def max_over_ranks(x: float, world: int) -> float:
@@ -389,6 +455,7 @@ def main():
     ap.add_argument("--variant", type=int, default=-1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-input", action="store_true", help="skip the input-path kernel measurement")
     ap.add_argument("--workload", choices=["config1", "config2", "config3", "config4", "config5"], default="config2")
     ap.add_argument("--band", type=int, choices=[0, 1, 2], default=0,
                     help="band mode for global workloads: 1 learned (shipped weights), 2 straight")

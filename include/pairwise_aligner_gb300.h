@@ -309,6 +309,63 @@ typedef struct pa_roofline {
 } pa_roofline;
 pa_status pa_measure_roofline(pa_ctx *ctx, pa_roofline *out);
 
+/* ---- Input path ------------------------------------------------------------
+ * Symbol -> rank conversion (alphabet_conversion/alphabet_rank_map_scalar.hpp and
+ * alphabet_rank_map_simd.hpp:31-117): symbols[r] gets rank r (a repeated symbol
+ * keeps its last rank, as the reference's fill loop does), every other byte -1.
+ * n_symbols 1..127 (an empty list is PA_ERR_INVALID_ARGUMENT, as the reference
+ * throws std::invalid_argument).  Device buffers of n bytes, asynchronous on
+ * `stream` (NULL: the context's stream); *n_invalid (host, may be NULL) receives
+ * the number of bytes without a rank, which makes the call synchronous. */
+pa_status pa_rank_map_device(pa_ctx *ctx, const uint8_t *symbols, uint32_t n_symbols,
+                             const uint8_t *d_in, uint64_t n, int8_t *d_out, void *stream,
+                             uint64_t *n_invalid);
+
+/* 2-bit DNA packing (no counterpart in the reference).  Base i of a stream is
+ * bits 2(i mod 16) .. 2(i mod 16)+1 of word i / 16; A/a = 0, C/c = 1, G/g = 2,
+ * T/t = 3.  Any other byte is counted in *n_invalid and packed as
+ * ((b >> 1) ^ (b >> 2)) & 3.  Unused bits of the last word are 0.
+ * pa_pack_2bit_host runs on the calling thread (host buffers, the encoder for
+ * files and callers that keep DNA packed); the _device forms run on `stream`
+ * (NULL: the context's stream; synchronous when n_invalid is given).  Unpacking
+ * writes bases [first_base, first_base + n) of the stream as the upper-case
+ * letters ACGT. */
+pa_status pa_pack_2bit_host(const uint8_t *in, uint64_t n, uint32_t *out_words, uint64_t *n_invalid);
+pa_status pa_pack_2bit_device(pa_ctx *ctx, const uint8_t *d_in, uint64_t n, uint32_t *d_words,
+                              void *stream, uint64_t *n_invalid);
+pa_status pa_unpack_2bit_device(pa_ctx *ctx, const uint32_t *d_words, uint64_t first_base, uint64_t n,
+                                uint8_t *d_out, void *stream);
+
+/* pa_align_batch over 2-bit packed host sequences: pair k is bases
+ * [off1[k], off1[k+1]) of the packed stream seq1_words against bases
+ * [off2[k], off2[k+1]) of seq2_words.  Only the packed words cross to the
+ * device (a quarter of the bytes); they are unpacked there into ACGT and
+ * aligned exactly as pa_align_batch would align the letters. */
+pa_status pa_align_batch_packed(pa_ctx *ctx, const pa_config *config,
+                                const uint32_t *seq1_words, const uint64_t *off1,
+                                const uint32_t *seq2_words, const uint64_t *off2,
+                                uint64_t n_pairs, pa_result *out, pa_stats *stats);
+
+/* FASTA / FASTQ reader (the record format of test/data/in.fastq; FASTA with
+ * sequences over several lines).  The format is taken from the first
+ * non-blank byte ('>' or '@').  Sequence bytes are kept as they are (no case
+ * change); line ends may be LF or CRLF; a FASTQ record is '@name', sequence
+ * line(s), '+' (optionally the name again), quality line(s) of the sequence's
+ * length.  On a malformed file the status is PA_ERR_INVALID_ARGUMENT and `err`
+ * (err_len bytes, may be NULL) holds the line number and the reason. */
+typedef struct pa_seqfile pa_seqfile;
+pa_status pa_seqfile_read(const char *path, pa_seqfile **out, char *err, size_t err_len);
+pa_status pa_seqfile_parse(const char *text, uint64_t len, pa_seqfile **out, char *err, size_t err_len);
+uint64_t pa_seqfile_count(const pa_seqfile *f);
+/* concatenated sequence bytes, and count + 1 offsets into them */
+const uint8_t *pa_seqfile_sequences(const pa_seqfile *f);
+const uint64_t *pa_seqfile_offsets(const pa_seqfile *f);
+/* FASTQ: the qualities, concatenated with the same offsets; FASTA: NULL */
+const uint8_t *pa_seqfile_qualities(const pa_seqfile *f);
+/* record i's name: the header line after '>' / '@', up to the line end */
+const char *pa_seqfile_name(const pa_seqfile *f, uint64_t i);
+void pa_seqfile_free(pa_seqfile *f);
+
 const char *pa_status_string(pa_status status);
 /* Message of the last error on this context (empty string if none). */
 const char *pa_last_error(const pa_ctx *ctx);

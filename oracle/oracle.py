@@ -182,3 +182,38 @@ def band_labels(cfg: OracleCfg, s1: bytes, s2: bytes) -> list[int]:
         tot = hf[:n] + hr[n - np.arange(n)]
         out.append(int(np.argmax(tot)) - r)
     return out
+
+
+# -- input path -----------------------------------------------------------------------------------
+
+def rank_table(symbols: bytes) -> np.ndarray:
+    """The reference's alphabet_rank_map_scalar (alphabet_conversion/alphabet_rank_map_scalar.hpp):
+    a 256-entry table, -1 everywhere, then rank r written for symbols[r] in list order (a repeated
+    symbol keeps its last rank).  An empty list is an error, as alphabet_rank_map_simd throws
+    std::invalid_argument for it (alphabet_rank_map_simd.hpp:61-63)."""
+    if len(symbols) == 0:
+        raise ValueError("the given set of valid symbols is empty")
+    tab = np.full(256, -1, dtype=np.int8)
+    for r, b in enumerate(bytes(symbols)):
+        tab[b] = r
+    return tab
+
+
+def rank_map(symbols: bytes, data: np.ndarray) -> np.ndarray:
+    """Ranks of every byte of `data` (int8, -1 for a byte that is not a symbol)."""
+    return rank_table(symbols)[np.asarray(data, dtype=np.uint8)]
+
+
+def pack_2bit(data: np.ndarray) -> tuple[np.ndarray, int]:
+    """2-bit DNA packing restated with numpy: base i at bits 2(i mod 16) of word i // 16, code
+    ((b >> 1) ^ (b >> 2)) & 3 (A/a 0, C/c 1, G/g 2, T/t 3); returns (words, count of bytes whose
+    b | 0x20 is not one of a c g t)."""
+    b = np.asarray(data, dtype=np.uint8)
+    n = len(b)
+    code = (((b >> 1) ^ (b >> 2)) & 3).astype(np.uint32)
+    pad = np.zeros((-n) % 16, dtype=np.uint32)
+    c = np.concatenate([code, pad]).reshape(-1, 16)
+    words = (c << (2 * np.arange(16, dtype=np.uint32))).sum(axis=1, dtype=np.uint64).astype(np.uint32)
+    lower = b | 0x20
+    bad = int(np.count_nonzero(~np.isin(lower, np.frombuffer(b"acgt", dtype=np.uint8))))
+    return words, bad

@@ -6,9 +6,9 @@ A drop-in for rrahn/pairwise_aligner's affine global/local score DP: the same
 and ``compute(...)`` results with ``score()``, computed by hand-written CUDA
 kernels through the C ABI of include/pairwise_aligner_gb300.h.
 """
-from . import cfg
+from . import cfg, seqio
 from .aligner import Aligner, AlignerResult, Context, RESULT_DTYPE, pack
 from ._lib import PaError
 
-__all__ = ["cfg", "Aligner", "AlignerResult", "Context", "RESULT_DTYPE", "pack", "PaError"]
+__all__ = ["cfg", "seqio", "Aligner", "AlignerResult", "Context", "RESULT_DTYPE", "pack", "PaError"]
 __version__ = "0.1.0"

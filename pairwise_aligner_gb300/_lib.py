@@ -157,6 +157,27 @@ SIGNATURES = {
     "pa_align_batch_banded": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.POINTER(PaStats)], ctypes.c_int),
+    "pa_rank_map_device": ([_ctxp, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
+                            ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    "pa_pack_2bit_host": ([ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)],
+                          ctypes.c_int),
+    "pa_pack_2bit_device": ([_ctxp, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                             ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    "pa_unpack_2bit_device": ([_ctxp, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
+                               ctypes.c_void_p], ctypes.c_int),
+    "pa_align_batch_packed": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                               ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(PaStats)],
+                              ctypes.c_int),
+    "pa_seqfile_read": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p, ctypes.c_size_t],
+                        ctypes.c_int),
+    "pa_seqfile_parse": ([ctypes.c_char_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p,
+                          ctypes.c_size_t], ctypes.c_int),
+    "pa_seqfile_count": ([ctypes.c_void_p], ctypes.c_uint64),
+    "pa_seqfile_sequences": ([ctypes.c_void_p], ctypes.c_void_p),
+    "pa_seqfile_offsets": ([ctypes.c_void_p], ctypes.c_void_p),
+    "pa_seqfile_qualities": ([ctypes.c_void_p], ctypes.c_void_p),
+    "pa_seqfile_name": ([ctypes.c_void_p, ctypes.c_uint64], ctypes.c_char_p),
+    "pa_seqfile_free": ([ctypes.c_void_p], None),
     "pa_get_tuning": ([_ctxp, ctypes.POINTER(PaTuning)], ctypes.c_int),
     "pa_set_tuning": ([_ctxp, ctypes.POINTER(PaTuning)], ctypes.c_int),
     "pa_status_string": ([ctypes.c_int], ctypes.c_char_p),

@@ -248,6 +248,34 @@ class Aligner:
             self.last_stats = self._stats_dict(st)
         return out[:n]
 
+    def compute_packed(self, words1: np.ndarray, off1: np.ndarray, words2: np.ndarray, off2: np.ndarray,
+                       stats: bool = True, out: np.ndarray | None = None) -> np.ndarray:
+        """As compute_arrays, for 2-bit packed DNA (``seqio.pack_2bit``): offsets count bases."""
+        n = len(off1) - 1
+        if len(off2) - 1 != n:
+            raise ValueError("both sequence collections must hold the same number of sequences")
+        words1 = np.ascontiguousarray(words1, dtype=np.uint32)
+        words2 = np.ascontiguousarray(words2, dtype=np.uint32)
+        off1 = np.ascontiguousarray(off1, dtype=np.uint64)
+        off2 = np.ascontiguousarray(off2, dtype=np.uint64)
+        for w, o in ((words1, off1), (words2, off2)):
+            if n and len(w) * 16 < int(o[-1]):
+                raise ValueError("the packed words end before the last offset")
+        if out is None:
+            out = np.zeros(max(n, 1), dtype=RESULT_DTYPE)
+        elif out.dtype != RESULT_DTYPE or len(out) < n or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous RESULT_DTYPE array of at least n_pairs entries")
+        st = _lib.PaStats()
+        ctx = self.context
+        cfg = self.c_config()
+        rc = ctx.lib.pa_align_batch_packed(ctx.ptr, ctypes.byref(cfg), words1.ctypes.data, off1.ctypes.data,
+                                           words2.ctypes.data, off2.ctypes.data, n, out.ctypes.data,
+                                           ctypes.byref(st) if stats else None)
+        _lib.check(rc, ctx.ptr)
+        if stats:
+            self.last_stats = self._stats_dict(st)
+        return out[:n]
+
     def compute_banded(self, seq1: np.ndarray, off1: np.ndarray, seq2: np.ndarray, off2: np.ndarray,
                        bands: np.ndarray) -> np.ndarray:
         """Band mode with caller-given bands: (n_pairs, 10) int32 rows diag[8], w_start, w_min."""

@@ -85,6 +85,8 @@ struct pa_ctx {
     // substitution matrix (PA_SCORE_MATRIX): int8 rank per byte (-1: not a symbol), int32 scores
     DevBuf mat_rank, mat_scores;
     int32_t mat_dim = 0, mat_max = 0, mat_min = 0;
+    // input path: rank table, invalid-symbol counter, packed staging of pa_align_batch_packed
+    DevBuf io_tab, io_ctr, in_words1, in_words2;
 };
 
 namespace {
@@ -201,6 +203,13 @@ void dp_launch_v3(bool, bool, int, int, cudaStream_t, const DpLaunch &, const Dp
 void dp_launch_v4(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v5(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v6(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
+
+void rank_map_launch(const uint8_t *in, uint64_t n, int8_t *out, const int8_t *table, unsigned long long *invalid,
+                     int sm_count, cudaStream_t st);
+void pack_2bit_launch(const uint8_t *in, uint64_t n, uint32_t *words, unsigned long long *invalid, int sm_count,
+                      cudaStream_t st);
+void unpack_2bit_launch(const uint32_t *words, uint64_t first_base, uint64_t n, uint8_t *out, int sm_count,
+                        cudaStream_t st);
 
 int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
 {
@@ -1007,7 +1016,8 @@ pa_status pa_destroy(pa_ctx *c)
                       &c->in_seq1, &c->in_off1, &c->in_seq2, &c->in_off2, &c->in_out,
                       &c->band_spec, &c->band_win, &c->band_code, &c->band_bsum, &c->band_ctr, &c->band_in,
                       &c->mlp_feat, &c->mlp_x, &c->mlp_h1, &c->mlp_h2, &c->mlp_out,
-                      &c->ring, &c->rerun_long, &c->mat_rank, &c->mat_scores};
+                      &c->ring, &c->rerun_long, &c->mat_rank, &c->mat_scores,
+                      &c->io_tab, &c->io_ctr, &c->in_words1, &c->in_words2};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     for (DevBuf &b : c->band_list)
@@ -1055,7 +1065,8 @@ pa_status pa_align_batch_device(pa_ctx *ctx, const pa_config *config, const uint
 
 static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1, const uint64_t *off1,
                             const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, pa_result *out,
-                            pa_stats *stats, const int32_t *bands);
+                            pa_stats *stats, const int32_t *bands, const uint32_t *words1 = nullptr,
+                            const uint32_t *words2 = nullptr);
 
 pa_status pa_align_batch(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1, const uint64_t *off1,
                          const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, pa_result *out,
@@ -1182,18 +1193,23 @@ pa_status pa_set_band_model(pa_ctx *ctx, const float *w1, const float *b1, const
     return PA_OK;
 }
 
+// Host buffers in, host results out.  With words1 / words2 the sequences are 2-bit packed host
+// streams (offsets count bases): the packed words are copied and unpacked on the device.
 static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1, const uint64_t *off1,
                             const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, pa_result *out,
-                            pa_stats *stats, const int32_t *bands)
+                            pa_stats *stats, const int32_t *bands, const uint32_t *words1,
+                            const uint32_t *words2)
 {
     if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    const bool packed = words1 != nullptr;
     if (n_pairs == 0) {
         DpParams P; ClassCfg C;
         pa_status s = check_config(ctx, config, P, C);
         if (stats) std::memset(stats, 0, sizeof(*stats));
         return s;
     }
-    if (!seq1 || !off1 || !seq2 || !off2 || !out) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null buffer");
+    if ((packed ? (!words1 || !words2) : (!seq1 || !seq2)) || !off1 || !off2 || !out)
+        return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null buffer");
     int64_t long_m = 0;
     for (uint64_t k = 0; k < n_pairs; ++k) {
         if (off1[k + 1] < off1[k] || off2[k + 1] < off2[k])
@@ -1220,9 +1236,27 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
     // the two sequence sets go over two copy engines at once (side stream joins before the DP)
     PA_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
     PA_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-    if (b1) PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_seq1.p, seq1 + base1, b1, cudaMemcpyHostToDevice, ctx->side));
+    if (packed) {
+        // words [base / 16, (base + bytes + 15) / 16) of each stream, unpacked into the staging bytes
+        const uint64_t q1 = base1 >> 4, nw1 = ((base1 + b1 + 15) >> 4) - q1;
+        const uint64_t q2 = base2 >> 4, nw2 = ((base2 + b2 + 15) >> 4) - q2;
+        if ((s = ensure(ctx, ctx->in_words1, nw1 * 4))) return s;
+        if ((s = ensure(ctx, ctx->in_words2, nw2 * 4))) return s;
+        if (b1) {
+            PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_words1.p, words1 + q1, nw1 * 4, cudaMemcpyHostToDevice, ctx->side));
+            unpack_2bit_launch((const uint32_t *)ctx->in_words1.p, base1 & 15, b1, (uint8_t *)ctx->in_seq1.p,
+                               ctx->sm_count, ctx->side);
+        }
+        if (b2) {
+            PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_words2.p, words2 + q2, nw2 * 4, cudaMemcpyHostToDevice, st));
+            unpack_2bit_launch((const uint32_t *)ctx->in_words2.p, base2 & 15, b2, (uint8_t *)ctx->in_seq2.p,
+                               ctx->sm_count, st);
+        }
+    } else {
+        if (b1) PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_seq1.p, seq1 + base1, b1, cudaMemcpyHostToDevice, ctx->side));
+        if (b2) PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_seq2.p, seq2 + base2, b2, cudaMemcpyHostToDevice, st));
+    }
     PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off1.p, h1, (n_pairs + 1) * 8, cudaMemcpyHostToDevice, ctx->side));
-    if (b2) PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_seq2.p, seq2 + base2, b2, cudaMemcpyHostToDevice, st));
     PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off2.p, h2, (n_pairs + 1) * 8, cudaMemcpyHostToDevice, st));
     PA_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
     PA_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
@@ -1242,6 +1276,83 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
     PA_CUDA(ctx, cudaMemcpyAsync(out, ctx->in_out.p, n_pairs * sizeof(pa_result), cudaMemcpyDeviceToHost, st));
     PA_CUDA(ctx, cudaStreamSynchronize(st));
     return read_stats(ctx, stats);
+}
+
+pa_status pa_align_batch_packed(pa_ctx *ctx, const pa_config *config, const uint32_t *seq1_words,
+                                const uint64_t *off1, const uint32_t *seq2_words, const uint64_t *off2,
+                                uint64_t n_pairs, pa_result *out, pa_stats *stats)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    if (n_pairs && (!seq1_words || !seq2_words)) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null buffer");
+    static const uint32_t kNone = 0;     // n_pairs == 0: any non-null pointer selects the packed path
+    return align_host(ctx, config, nullptr, off1, nullptr, off2, n_pairs, out, stats, nullptr,
+                      seq1_words ? seq1_words : &kNone, seq2_words ? seq2_words : &kNone);
+}
+
+// The input-path kernels on the caller's stream (or the context's); a non-null n_invalid waits
+// for the count.  The counter belongs to the context: calls on one context are not concurrent.
+static pa_status io_counter(pa_ctx *ctx, cudaStream_t st)
+{
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, PA_ERR_CUDA, "cudaSetDevice");
+    pa_status s = ensure(ctx, ctx->io_ctr, 8);
+    if (s) return s;
+    PA_CUDA(ctx, cudaMemsetAsync(ctx->io_ctr.p, 0, 8, st));
+    return PA_OK;
+}
+
+static pa_status io_finish(pa_ctx *ctx, cudaStream_t st, uint64_t *n_invalid)
+{
+    PA_CUDA(ctx, cudaGetLastError());
+    if (n_invalid) {
+        unsigned long long v = 0;
+        PA_CUDA(ctx, cudaMemcpyAsync(&v, ctx->io_ctr.p, 8, cudaMemcpyDeviceToHost, st));
+        PA_CUDA(ctx, cudaStreamSynchronize(st));
+        *n_invalid = v;
+    }
+    return PA_OK;
+}
+
+pa_status pa_rank_map_device(pa_ctx *ctx, const uint8_t *symbols, uint32_t n_symbols, const uint8_t *d_in,
+                             uint64_t n, int8_t *d_out, void *stream, uint64_t *n_invalid)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    if (!symbols || n_symbols == 0) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "the symbol list is empty");
+    if (n_symbols > 127) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "at most 127 symbols (int8 ranks)");
+    if (n && (!d_in || !d_out)) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null buffer");
+    int8_t table[256];
+    std::memset(table, -1, sizeof(table));
+    for (uint32_t r = 0; r < n_symbols; ++r) table[symbols[r]] = (int8_t)r;   // a repeat keeps its last rank
+    const cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    pa_status s;
+    if ((s = io_counter(ctx, st)) || (s = ensure(ctx, ctx->io_tab, 256))) return s;
+    PA_CUDA(ctx, cudaMemcpyAsync(ctx->io_tab.p, table, 256, cudaMemcpyHostToDevice, st));
+    PA_CUDA(ctx, cudaStreamSynchronize(st));      // `table` is a stack array
+    if (n) rank_map_launch(d_in, n, d_out, (const int8_t *)ctx->io_tab.p, (unsigned long long *)ctx->io_ctr.p,
+                           ctx->sm_count, st);
+    return io_finish(ctx, st, n_invalid);
+}
+
+pa_status pa_pack_2bit_device(pa_ctx *ctx, const uint8_t *d_in, uint64_t n, uint32_t *d_words, void *stream,
+                              uint64_t *n_invalid)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    if (n && (!d_in || !d_words)) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null buffer");
+    const cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    pa_status s;
+    if ((s = io_counter(ctx, st))) return s;
+    if (n) pack_2bit_launch(d_in, n, d_words, (unsigned long long *)ctx->io_ctr.p, ctx->sm_count, st);
+    return io_finish(ctx, st, n_invalid);
+}
+
+pa_status pa_unpack_2bit_device(pa_ctx *ctx, const uint32_t *d_words, uint64_t first_base, uint64_t n,
+                                uint8_t *d_out, void *stream)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    if (n && (!d_words || !d_out)) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null buffer");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, PA_ERR_CUDA, "cudaSetDevice");
+    const cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    if (n) unpack_2bit_launch(d_words, first_base, n, d_out, ctx->sm_count, st);
+    return io_finish(ctx, st, nullptr);
 }
 
 pa_status pa_align_one_to_many(pa_ctx *ctx, const pa_config *config, const uint8_t *query, uint64_t query_len,
