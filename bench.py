@@ -396,6 +396,7 @@ def input_kernels(dev, stream, ctx, n: int = 1 << 30, reps: int = 5) -> dict:
             "unpack_2bit": (lambda: seqio.unpack_2bit_device(ctx, words, 0, n, back), n // 4 + n),
             "rank_map": (lambda: seqio.rank_map_device(ctx, b"ACGTN", letters, ranks), 2 * n)}
     peak = hbm_peak()
+    stream.wait_stream(torch.cuda.current_stream())          # the inputs were made on torch's stream
     with torch.cuda.stream(stream):
         for name, (fn, nbytes) in jobs.items():
             fn()

@@ -1,7 +1,7 @@
 // pa_input.cu -- the input path around the DP: symbol -> rank conversion, 2-bit
 // packing of DNA (host encoder, device encoder and decoder), and the FASTA /
 // FASTQ reader.  The kernels are byte streams bound by HBM bandwidth: each
-// thread moves 16 input bytes per step with one vector load, grids are a
+// thread keeps kUnroll 16-byte vector loads in flight per step, grids are a
 // multiple of the SM count, and no kernel reads a byte twice.
 #include <cuda_runtime.h>
 
@@ -14,6 +14,8 @@
 #include "../../include/pairwise_aligner_gb300.h"
 
 namespace pa {
+
+constexpr int kUnroll = 4;     // independent 16-byte loads in flight per thread
 
 // ---------------------------------------------------------------------------------------------
 // rank map: the reference's alphabet_rank_map_scalar keeps a 256-entry table (-1 for bytes that
@@ -53,16 +55,26 @@ __global__ void __launch_bounds__(256) k_rank_map(const uint8_t *__restrict__ in
     uint64_t done = 0;
     if (vec) {
         const uint64_t nv = n >> 4;
-        for (uint64_t v = tid; v < nv; v += nth) {
-            const uint4 x = __ldcs(reinterpret_cast<const uint4 *>(in) + v);
-            uint4 y;
-            y.x = rank4(tab, lane, x.x);
-            y.y = rank4(tab, lane, x.y);
-            y.z = rank4(tab, lane, x.z);
-            y.w = rank4(tab, lane, x.w);
-            bad += __popc(y.x & 0x80808080u) + __popc(y.y & 0x80808080u) + __popc(y.z & 0x80808080u) +
-                   __popc(y.w & 0x80808080u);
-            __stcs(reinterpret_cast<uint4 *>(out) + v, y);
+        for (uint64_t v0 = tid; v0 < nv; v0 += kUnroll * nth) {
+            uint4 x[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const uint64_t v = v0 + u * nth;
+                x[u] = v < nv ? __ldcs(reinterpret_cast<const uint4 *>(in) + v) : make_uint4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const uint64_t v = v0 + u * nth;
+                if (v >= nv) break;
+                uint4 y;
+                y.x = rank4(tab, lane, x[u].x);
+                y.y = rank4(tab, lane, x[u].y);
+                y.z = rank4(tab, lane, x[u].z);
+                y.w = rank4(tab, lane, x[u].w);
+                bad += __popc(y.x & 0x80808080u) + __popc(y.y & 0x80808080u) + __popc(y.z & 0x80808080u) +
+                       __popc(y.w & 0x80808080u);
+                __stcs(reinterpret_cast<uint4 *>(out) + v, y);
+            }
         }
         done = nv << 4;
     }
@@ -84,10 +96,12 @@ __global__ void __launch_bounds__(256) k_rank_map(const uint8_t *__restrict__ in
 __device__ __forceinline__ uint32_t pack4(uint32_t w, unsigned &bad)
 {
     const uint32_t x = ((w >> 1) ^ (w >> 2)) & 0x03030303u;          // codes at bits 0, 8, 16, 24
-    const uint32_t lower = w | 0x20202020u;
-    const uint32_t ok = __vcmpeq4(lower, 0x61616161u) | __vcmpeq4(lower, 0x63636363u) |
-                        __vcmpeq4(lower, 0x67676767u) | __vcmpeq4(lower, 0x74747474u);
-    bad += __popc(~ok) >> 3;
+    // the lower-case letter each code stands for (one PRMT); a byte is valid when b | 0x20 is it
+    const uint32_t sel = (x & 3u) | ((x >> 4) & 0x30u) | ((x >> 8) & 0x300u) | ((x >> 12) & 0x3000u);
+    const uint32_t diff = (w | 0x20202020u) ^ __byte_perm(0x74676361u, 0u, sel);
+    // bit 7 of a byte of z is set exactly when that byte of diff is zero (no carries between bytes)
+    const uint32_t z = ~(((diff & 0x7f7f7f7fu) + 0x7f7f7f7fu) | diff | 0x7f7f7f7fu);
+    bad += 4u - __popc(z);
     const uint32_t y = x | (x >> 6);                                   // codes at bits 0-3, 16-19
     return (y & 0xfu) | ((y >> 12) & 0xf0u);
 }
@@ -101,12 +115,28 @@ __global__ void __launch_bounds__(256) k_pack_2bit(const uint8_t *__restrict__ i
     const uint64_t nfull = n >> 4, nwords = (n + 15) >> 4;
     const bool vec = (reinterpret_cast<uintptr_t>(in) & 15) == 0;
     unsigned bad = 0;
-    for (uint64_t v = tid; v < nwords; v += nth) {
+    uint64_t first_slow = 0;
+    if (vec) {
+        for (uint64_t v0 = tid; v0 < nfull; v0 += kUnroll * nth) {
+            uint4 x[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const uint64_t v = v0 + u * nth;
+                x[u] = v < nfull ? __ldcs(reinterpret_cast<const uint4 *>(in) + v) : make_uint4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const uint64_t v = v0 + u * nth;
+                if (v >= nfull) break;
+                words[v] = pack4(x[u].x, bad) | (pack4(x[u].y, bad) << 8) | (pack4(x[u].z, bad) << 16) |
+                           (pack4(x[u].w, bad) << 24);
+            }
+        }
+        first_slow = nfull;
+    }
+    for (uint64_t v = first_slow + tid; v < nwords; v += nth) {
         uint32_t w[4];
-        if (v < nfull && vec) {
-            const uint4 x = __ldcs(reinterpret_cast<const uint4 *>(in) + v);
-            w[0] = x.x; w[1] = x.y; w[2] = x.z; w[3] = x.w;
-        } else {
+        {
             // unaligned input or the last partial word: byte loads; missing bytes act as 'A'
             // (code 0) and are not counted
             const uint64_t base = v << 4;
@@ -145,13 +175,21 @@ __global__ void __launch_bounds__(256) k_unpack_2bit(const uint32_t *__restrict_
     const uint32_t sh = (uint32_t)(first_base & 15) * 2;
     const uint64_t last_word = n ? (first_base + n - 1) >> 4 : 0;
     const bool vec = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
-    for (uint64_t t = tid; (t << 4) < n; t += nth) {
-        const uint64_t q = (first_base >> 4) + t;
-        uint32_t bits = __ldg(words + q);
-        if (sh) {
-            const uint32_t hi = q + 1 <= last_word ? __ldg(words + q + 1) : 0u;
-            bits = __funnelshift_r(bits, hi, sh);
+    const uint64_t nt = (n + 15) >> 4;
+    for (uint64_t t0 = tid; t0 < nt; t0 += kUnroll * nth) {
+        uint32_t lo[kUnroll], hi[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const uint64_t t = t0 + u * nth;
+            const uint64_t q = (first_base >> 4) + t;
+            lo[u] = t < nt ? __ldg(words + q) : 0u;
+            hi[u] = (t < nt && sh && q + 1 <= last_word) ? __ldg(words + q + 1) : 0u;
         }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+        const uint64_t t = t0 + u * nth;
+        if (t >= nt) break;
+        const uint32_t bits = sh ? __funnelshift_r(lo[u], hi[u], sh) : lo[u];
         uint4 y;
         y.x = unpack4(bits & 0xffu);
         y.y = unpack4((bits >> 8) & 0xffu);
@@ -163,6 +201,7 @@ __global__ void __launch_bounds__(256) k_unpack_2bit(const uint32_t *__restrict_
         } else {
             const uint32_t v[4] = {y.x, y.y, y.z, y.w};
             for (int b = 0; b < 16 && o + b < n; ++b) out[o + b] = (uint8_t)(v[b >> 2] >> (8 * (b & 3)));
+        }
         }
     }
 }
