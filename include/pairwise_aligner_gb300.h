@@ -106,7 +106,7 @@ typedef struct pa_options {
     int32_t blocks_per_sm;      /* persistent grid occupancy: 0 auto                       */
     int32_t use_graphs;         /* 0 auto(on), 1 on, -1 off                                */
     int32_t autotune;           /* 0 off, 1 on first use                                   */
-    int32_t kernel_variant;     /* inner-loop form: -1 auto (per-method tuning), else 0..6 (pa_tuning) */
+    int32_t kernel_variant;     /* inner-loop form: -1 auto (per-method tuning), else 0..8 (pa_tuning) */
     int32_t reserved[2];
 } pa_options;
 
@@ -277,7 +277,8 @@ pa_status pa_align_batch_banded(pa_ctx *ctx, const pa_config *config,
  * shapes are compile-time lane widths, simd/simd_base.hpp:28-57).
  * variant: inner-loop form of the DP (0 three-operand max, 1 short chain,
  * 2 three-operand with at most 85 registers, 3 branch-free top input with L1
- * prefetch, 4 as 3 with a two-op vertical-gap chain); group_threads: lanes
+ * prefetch, 4 as 3 with a two-op vertical-gap chain, 5 / 6 as 3 / 4 with one
+ * prefetch per 8 columns, 7 / 8 as 3 / 4 without the score-table prefetch); group_threads: lanes
  * per pair group (1..32, power of two).  Index 0 = local, 1 = global. */
 typedef struct pa_tuning {
     int32_t variant_s16[2];

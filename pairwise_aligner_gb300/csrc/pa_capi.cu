@@ -33,7 +33,7 @@ namespace {
 constexpr int kR = 16;             // rows per thread per lane
 constexpr int64_t kDefaultRingM = 65536;   // device entry points: CTA mode up to this sequence1 length
 constexpr int kDefaultG = 8;       // threads per group
-constexpr int kVariants = 7;       // inner-loop variants (pa_kern_v*.cu)
+constexpr int kVariants = 9;       // inner-loop variants (pa_kern_v*.cu)
 
 struct DevBuf {
     void *p = nullptr;
@@ -196,6 +196,8 @@ int dp_occupancy_v3(bool lanes16, bool gen, int mode);
 int dp_occupancy_v4(bool lanes16, bool gen, int mode);
 int dp_occupancy_v5(bool lanes16, bool gen, int mode);
 int dp_occupancy_v6(bool lanes16, bool gen, int mode);
+int dp_occupancy_v7(bool lanes16, bool gen, int mode);
+int dp_occupancy_v8(bool lanes16, bool gen, int mode);
 void dp_launch_v0(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v1(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v2(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
@@ -203,6 +205,8 @@ void dp_launch_v3(bool, bool, int, int, cudaStream_t, const DpLaunch &, const Dp
 void dp_launch_v4(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v5(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 void dp_launch_v6(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
+void dp_launch_v7(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
+void dp_launch_v8(bool, bool, int, int, cudaStream_t, const DpLaunch &, const DpParams &);
 
 void rank_map_launch(const uint8_t *in, uint64_t n, int8_t *out, const int8_t *table, unsigned long long *invalid,
                      int sm_count, cudaStream_t st);
@@ -219,6 +223,8 @@ int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
     if (variant == 4) return dp_occupancy_v4(lanes16, gen, mode);
     if (variant == 5) return dp_occupancy_v5(lanes16, gen, mode);
     if (variant == 6) return dp_occupancy_v6(lanes16, gen, mode);
+    if (variant == 7) return dp_occupancy_v7(lanes16, gen, mode);
+    if (variant == 8) return dp_occupancy_v8(lanes16, gen, mode);
     return dp_occupancy_v0(lanes16, gen, mode);
 }
 
@@ -250,6 +256,8 @@ void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStre
     else if (variant == 4) dp_launch_v4(lanes16, gen, mode, grid, st, L, P);
     else if (variant == 5) dp_launch_v5(lanes16, gen, mode, grid, st, L, P);
     else if (variant == 6) dp_launch_v6(lanes16, gen, mode, grid, st, L, P);
+    else if (variant == 7) dp_launch_v7(lanes16, gen, mode, grid, st, L, P);
+    else if (variant == 8) dp_launch_v8(lanes16, gen, mode, grid, st, L, P);
     else dp_launch_v0(lanes16, gen, mode, grid, st, L, P);
 }
 }  // namespace pa
@@ -986,8 +994,8 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
         return PA_ERR_CUDA;
     }
     // defaults measured on GB300 (262,144 pairs of 64..512 bp): local s16x2 is fastest with
-    // variant 3, global with variant 4; 8 lanes per group
-    c->tuning = pa_tuning{{3, 4}, {0, 4}, {8, 8}, {8, 8}, {0.0, 0.0}};
+    // variant 7, global with variant 4; 8 lanes per group
+    c->tuning = pa_tuning{{7, 4}, {0, 4}, {8, 8}, {8, 8}, {0.0, 0.0}};
     if (c->opt.group_threads) {
         int g = c->opt.group_threads;
         if (g < 1 || g > 32 || (g & (g - 1))) { pa_destroy(c); return PA_ERR_INVALID_ARGUMENT; }
@@ -1508,7 +1516,7 @@ pa_status pa_set_tuning(pa_ctx *ctx, const pa_tuning *t)
     for (int m = 0; m < 2; ++m)
         if (!valid_variant(t->variant_s16[m]) || !valid_variant(t->variant_s32[m]) || !valid_G(t->group_threads_s16[m]) ||
             !valid_G(t->group_threads_s32[m]))
-            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "tuning: variant must be 0..6 and group_threads 1..32, power of two");
+            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "tuning: variant must be 0..8 and group_threads 1..32, power of two");
     ctx->tuning = *t;
     ctx->fixed_G = ctx->fixed_variant = false;
     return PA_OK;
@@ -1525,7 +1533,7 @@ pa_status pa_autotune(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1,
     std::vector<pa_result> res(std::max<uint64_t>(n_pairs, 1));
     double best = 1e300;
     pa_tuning choice = saved;
-    static const int kCandidates[] = {0, 1, 3, 4, 5, 6};
+    static const int kCandidates[] = {0, 1, 3, 4, 5, 6, 7, 8};
     static const int kGroups[] = {4, 8, 16};
     for (int v : kCandidates)
         for (int g : kGroups) {

@@ -379,6 +379,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
     }
     constexpr bool TUNED = (VAR & 4) != 0;
     constexpr bool SPARSE = (VAR & 16) != 0;        // prefetches once per 8 columns, boundary included
+    constexpr bool TABLE_PF = (VAR & 32) == 0;      // L1 prefetch of the score tables 7 columns ahead
     const bool first_thread = t == 0;
     const bool top_border = first_thread && p == 0;
     const bool top_buffer = first_thread && p > 0;
@@ -405,7 +406,7 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
                     }
                     if (!SYNC && top_buffer && i + 32 <= iend) asm volatile("prefetch.global.L1 [%0];" ::"l"(w.bin + i + 32));
                 }
-            } else if (!GEN && i + 8 <= iend) {
+            } else if (TABLE_PF && !GEN && i + 8 <= iend) {
                 asm volatile("prefetch.global.L1 [%0];" ::"l"(w.qt[0] + min(i + 7, w.m[0])));
                 if (NL == 2) asm volatile("prefetch.global.L1 [%0];" ::"l"(w.qt[1] + min(i + 7, w.m[1])));
             }

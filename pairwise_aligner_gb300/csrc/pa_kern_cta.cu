@@ -1,6 +1,8 @@
 // pa_kern_cta.cu -- instantiations of the CTA-mode DP kernel (long pairs: the warps
 // of a block pipeline the passes of one pair).  Local mode uses the branch-free
-// top input with L1 prefetch, global modes add the two-op vertical-gap chain.
+// top input, global modes add the two-op vertical-gap chain; neither prefetches the
+// score tables (measured 1-4 % faster without on GB300: the tables are loaded one
+// column ahead and stay in L1).
 #include "pa_dp.cuh"
 
 namespace pa {
@@ -13,7 +15,7 @@ int occ_cta()
     static int per_sm = -1;
     if (per_sm < 0) {
         int v = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel_cta<V, kRowsCta, MODE, GEN, MODE == M_LOCAL ? 4 : 12>,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel_cta<V, kRowsCta, MODE, GEN, MODE == M_LOCAL ? 36 : 44>,
                                                       kBlock, 0);
         per_sm = v < 1 ? 1 : v;
     }
@@ -23,7 +25,7 @@ int occ_cta()
 template <class V, int MODE, bool GEN>
 void go_cta(int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
 {
-    dp_kernel_cta<V, kRowsCta, MODE, GEN, MODE == M_LOCAL ? 4 : 12><<<grid, kBlock, 0, st>>>(L, P);
+    dp_kernel_cta<V, kRowsCta, MODE, GEN, MODE == M_LOCAL ? 36 : 44><<<grid, kBlock, 0, st>>>(L, P);
 }
 
 template <class V, bool GEN>

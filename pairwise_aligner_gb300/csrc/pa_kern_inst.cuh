@@ -3,7 +3,8 @@
 // 1: short-chain H, 2 blocks/SM; 2: as 0 with at most 85 registers (3 blocks/SM);
 // 3: as 0 with a branch-free top input and L1 prefetch of the score tables;
 // 4: as 3 with the two-op vertical-gap chain; 5 and 6: as 3 and 4 with one prefetch per
-// 8 columns that also covers the pass-boundary row.
+// 8 columns that also covers the pass-boundary row; 7 and 8: as 3 and 4 without the
+// score-table prefetch.
 #ifndef PA_VARIANT
 #error "define PA_VARIANT"
 #endif
@@ -14,6 +15,8 @@ constexpr int kVarMath = PA_VARIANT == 1   ? 1
                          : PA_VARIANT == 4 ? 12
                          : PA_VARIANT == 5 ? 20
                          : PA_VARIANT == 6 ? 28
+                         : PA_VARIANT == 7 ? 36
+                         : PA_VARIANT == 8 ? 44
                                            : 0;
 constexpr int kVarMinB = PA_VARIANT == 2 ? 3 : 2;
 constexpr int kRows = 16;

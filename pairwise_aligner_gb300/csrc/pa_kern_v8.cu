@@ -1,0 +1,10 @@
+// pa_kern_v8.cu -- instantiations of dp_kernel for inner-loop variant 8.
+#include "pa_dp.cuh"
+#include "pa_launch.h"
+
+namespace pa {
+
+#define PA_VARIANT 8
+#include "pa_kern_inst.cuh"
+
+}  // namespace pa
