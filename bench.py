@@ -52,7 +52,7 @@ BAND_MODEL = os.path.join(REPO, "pairwise_aligner_gb300", "data", "band_model.np
 # DRAM bytes per cell of the s16x2 local DP kernel, from one ncu capture of its launch on the
 # first 32,768 pairs of this workload (dram__bytes_read.sum + dram__bytes_write.sum divided by
 # the launch's 2.7146e9 cells; the traffic grows with the cells).
-DRAM_BYTES_PER_CELL = (49.772288e6 + 4.112896e6) / 2714564472     # ncu capture, profiles/dp_kernel_s16x2_local_config2.md
+DRAM_BYTES_PER_CELL = (49.772288e6 + 4.112896e6) / 2714564472
 
 
 def env_rank():
