@@ -15,6 +15,7 @@ One step = one call of the hot path over the whole batch:
   e2e_packed -- the same through pa_align_batch_packed: 2-bit packed host streams
             (a quarter of the sequence bytes cross to the device; DNA workloads).
   input_path -- GB/s of the 2-bit pack / unpack and rank-map kernels on 1 GiB.
+  traceback -- with --traceback: GCUPS of pa_traceback_batch (alignment ops) on the batch.
   roofline -- the DP kernels' own duration (events inside the library) against
             the measured whole-chip rate of the cell-update instruction mix
             (pa_measure_roofline); HBM traffic against MEASURED_PEAKS.json.
@@ -333,6 +334,23 @@ def our_arm(args):
                       "d2h_bytes_per_step": d2h, "entry": "pa_align_batch_packed (2-bit host streams)"}
     input_path = input_kernels(dev, stream, ctx) if not args.no_input else None
 
+    # the traceback path (alignment ops) over the same batch, host buffers, checked against
+    # the score-only results
+    traceback = None
+    if args.traceback:
+        tb_res = None
+        al.compute_traceback_arrays(hs["seq1"], hs["off1"], hs["seq2"], hs["off2"])
+        dev_ms, t0 = [], time.perf_counter()
+        for _ in range(args.steps):
+            tb_res, tb_aln, _, _ = al.compute_traceback_arrays(hs["seq1"], hs["off1"], hs["seq2"], hs["off2"])
+            dev_ms.append(al.last_stats["device_ms"])
+        tb_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+        assert np.array_equal(tb_res["score"], res["score"]), "traceback and score-only results disagree"
+        traceback = {"value": round(replica_throughput(cells, tb_s * 1e3, world), 2), "unit": "GCUPS",
+                     "device_gcups": round(cells / (statistics.mean(dev_ms) * 1e-3) / 1e9, 2),
+                     "ms_per_step": round(tb_s * 1e3, 3), "mean_ops": round(float(tb_aln["n_ops"].mean()), 2),
+                     "entry": "pa_traceback_batch (host buffers; score, end, begin and ops of every pair)"}
+
     achieved = cells / (dp_ms * 1e-3) / 1e9
     peak_gcups = peak["s16x2_cells_per_s"] / 1e9
     alg_bytes = int(d["off1"][-1] + d["off2"][-1]) + 16 * n          # inputs read + results written
@@ -364,6 +382,8 @@ def our_arm(args):
         line["e2e_packed"] = e2e_packed
     if input_path:
         line["input_path"] = input_path
+    if traceback:
+        line["traceback"] = traceback
     if args.band:
         line["band"] = {k: st[k] for k in ("pairs_banded", "pairs_full_dp", "band_cells", "band_rounds")}
         line["band"]["options"] = ctx.band_options()
@@ -457,6 +477,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-input", action="store_true", help="skip the input-path kernel measurement")
+    ap.add_argument("--traceback", action="store_true", help="also time pa_traceback_batch on the batch")
     ap.add_argument("--workload", choices=["config1", "config2", "config3", "config4", "config5"], default="config2")
     ap.add_argument("--band", type=int, choices=[0, 1, 2], default=0,
                     help="band mode for global workloads: 1 learned (shipped weights), 2 straight")

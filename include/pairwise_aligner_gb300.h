@@ -310,6 +310,35 @@ typedef struct pa_roofline {
 } pa_roofline;
 pa_status pa_measure_roofline(pa_ctx *ctx, pa_roofline *out);
 
+/* ---- Traceback ---------------------------------------------------------------
+ * The optimal alignment, which the reference does not compute (its trackers carry
+ * "TODO: optimal_coordinate()"): for every pair the pa_result of pa_align_batch (same
+ * score and end cell) plus the begin cell and the path as SAM-style ops, one byte per
+ * alignment column: '=' equal symbols, 'X' different symbols, 'D' a symbol of
+ * sequence1 against a gap, 'I' a symbol of sequence2 against a gap.  The path runs
+ * from just after cell (begin1, begin2) to (end1, end2): ops hold end1 - begin1
+ * sequence1 symbols ('=', 'X', 'D') and end2 - begin2 sequence2 symbols ('=', 'X',
+ * 'I').  A free leading gap shows as a begin > 0; a penalised one as ops.  Ties: the
+ * diagonal before a gap along sequence1 ('D') before one along sequence2 ('I'); a gap
+ * opens unless extending it is strictly better; a local path starts after the last
+ * cell whose score is 0.  Local pairs with a score <= 0 (or an empty sequence) have
+ * no ops.  Host buffers, synchronous; ops must hold (off1[n] - off1[0]) + (off2[n] -
+ * off2[0]) bytes, pair k's at (off1[k] - off1[0]) + (off2[k] - off2[0]).  Device
+ * memory: 4 bits per cell, in chunks of pairs of at most 4 GiB (a pair needing more
+ * is PA_ERR_TOO_LARGE). */
+typedef struct pa_alignment {
+    int32_t begin1;
+    int32_t begin2;
+    uint32_t n_ops;
+    uint32_t reserved;
+} pa_alignment;
+
+pa_status pa_traceback_batch(pa_ctx *ctx, const pa_config *config,
+                             const uint8_t *seq1, const uint64_t *off1,
+                             const uint8_t *seq2, const uint64_t *off2,
+                             uint64_t n_pairs, pa_result *out, pa_alignment *alignments,
+                             uint8_t *ops, pa_stats *stats);
+
 /* ---- Input path ------------------------------------------------------------
  * Symbol -> rank conversion (alphabet_conversion/alphabet_rank_map_scalar.hpp and
  * alphabet_rank_map_simd.hpp:31-117): symbols[r] gets rank r (a repeated symbol

@@ -72,6 +72,9 @@ def lib():
         L.pa_oracle_simd_batch.argtypes = [ctypes.POINTER(OracleCfg), u8p, u64p, u8p, u64p, ctypes.c_uint64,
                                            i32p, ctypes.c_int]
         L.pa_oracle_simd_batch.restype = ctypes.c_int
+        L.pa_oracle_traceback.argtypes = [ctypes.POINTER(OracleCfg), u8p, ctypes.c_uint64, u8p, ctypes.c_uint64,
+                                          i64p, i64p, i64p, i64p, i64p, u8p, i64p]
+        L.pa_oracle_traceback.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -164,6 +167,46 @@ def row(cfg: OracleCfg, s1: bytes, s2: bytes, r: int) -> np.ndarray:
     if rc:
         raise RuntimeError(f"pa_oracle_row failed: {rc}")
     return out
+
+
+def traceback(cfg: OracleCfg, s1: bytes, s2: bytes):
+    """One pair -> (score, begin1, begin2, end1, end2, ops) with ops a bytes string of '=', 'X',
+    'I', 'D' in path order (the conventions are in pa_oracle_traceback's comment)."""
+    a = np.frombuffer(bytes(s1), dtype=np.uint8) if len(s1) else np.zeros(1, np.uint8)
+    b = np.frombuffer(bytes(s2), dtype=np.uint8) if len(s2) else np.zeros(1, np.uint8)
+    ops = np.zeros(len(s1) + len(s2) + 1, dtype=np.uint8)
+    v = [ctypes.c_int64() for _ in range(6)]
+    rc = lib().pa_oracle_traceback(ctypes.byref(cfg), _ptr(a, ctypes.c_uint8), len(s1), _ptr(b, ctypes.c_uint8),
+                                   len(s2), *[ctypes.byref(x) for x in v[:5]], _ptr(ops, ctypes.c_uint8),
+                                   ctypes.byref(v[5]))
+    if rc:
+        raise RuntimeError(f"pa_oracle_traceback failed: {rc}")
+    return v[0].value, v[1].value, v[2].value, v[3].value, v[4].value, ops[:v[5].value].tobytes()
+
+
+def rescore(cfg: OracleCfg, s1: bytes, s2: bytes, begin1: int, begin2: int, ops: bytes) -> int:
+    """Score of an op string: substitutions plus open + ext * length per maximal gap run.  With a
+    free leading gap the begin offset costs nothing; a penalised leading gap is part of the ops."""
+    i, j, total, run = begin1, begin2, 0, None
+    for op in ops.decode():
+        if op in "=X":
+            a, b = s1[i], s2[j]
+            if cfg.dim:
+                rank = cfg._keep[1]
+                total += int(cfg._keep[0][rank[a], rank[b]])
+            else:
+                total += cfg.match if a == b else cfg.mismatch
+            i += 1
+            j += 1
+            run = None
+        else:
+            total += cfg.gap_extension + (cfg.gap_open if run != op else 0)
+            run = op
+            if op == "D":
+                i += 1
+            else:
+                j += 1
+    return total
 
 
 def band_labels(cfg: OracleCfg, s1: bytes, s2: bytes) -> list[int]:

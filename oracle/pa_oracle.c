@@ -180,6 +180,98 @@ int pa_oracle_align(const pa_oracle_cfg *c, const uint8_t *s1, uint64_t m, const
     return PA_ORACLE_OK;
 }
 
+/* Traceback (beyond the reference, whose trackers report no coordinates or path):
+ * the optimal alignment as SAM-style ops over the same recurrence and end cell as
+ * pa_oracle_align.  Full int64 matrices, so for small cases only.
+ *
+ * States: H (any), P (a gap along sequence1: op 'D', consumes a_i), Q (a gap along
+ * sequence2: op 'I', consumes b_j).  P(i,j) = max(P(i-1,j) + ext, H(i-1,j) + open + ext),
+ * P(1,j) = H(0,j) + open + ext; Q likewise along j (the reference's vertical / horizontal
+ * gap cells, affine_dp_algorithm.hpp:149-155, borders affine_initialisation_strategy.hpp:38-51).
+ * Tie-break convention:
+ *   - H(i,j): local and H == 0 -> the path starts after (i,j); else the diagonal if it
+ *     attains H, else P, else Q;
+ *   - P / Q: the gap opens at the previous cell unless extending is strictly better;
+ *   - borders: (0,j) ends the path with j 'I' ops unless the leading row gap is free
+ *     (then the path begins at (0,j)); (i,0) likewise with 'D' and the leading column.
+ * '=' when the aligned symbols are equal, 'X' otherwise (with a matrix too).
+ * ops receives n_ops <= m + n characters in path order; begin = the 0-based cell the
+ * path starts after; end = the same end cell as pa_oracle_align (0,0 and no ops when the
+ * local score is <= 0 or a sequence is empty). */
+int pa_oracle_traceback(const pa_oracle_cfg *c, const uint8_t *s1, uint64_t m, const uint8_t *s2, uint64_t n,
+                        int64_t *score, int64_t *begin1, int64_t *begin2, int64_t *end1, int64_t *end2,
+                        uint8_t *ops, int64_t *n_ops)
+{
+    if (!c || !score || !begin1 || !begin2 || !end1 || !end2 || !ops || !n_ops) return PA_ORACLE_EINVAL;
+    int rc = pa_oracle_align(c, s1, m, s2, n, score, end1, end2);
+    if (rc) return rc;
+    *begin1 = *begin2 = 0;
+    *n_ops = 0;
+    const int local = c->local != 0;
+    if (local && (m == 0 || n == 0 || *score <= 0)) return PA_ORACLE_OK;
+    const int first_col_free = local || c->first_column_free;
+    const int first_row_free = local || c->first_row_free;
+    const int64_t goe = (int64_t)c->gap_open + c->gap_extension, ext = c->gap_extension;
+    const uint64_t W = n + 1;
+    int64_t *H = (int64_t *)malloc(sizeof(int64_t) * (m + 1) * W);
+    int64_t *P = (int64_t *)malloc(sizeof(int64_t) * (m + 1) * W);
+    int64_t *Q = (int64_t *)malloc(sizeof(int64_t) * (m + 1) * W);
+    if (!H || !P || !Q) { free(H); free(P); free(Q); return PA_ORACLE_ENOMEM; }
+    for (uint64_t j = 0; j <= n; ++j) { int64_t g; border_cell(c, first_row_free, j, &H[j], &g); P[j] = g; Q[j] = g; }
+    for (uint64_t i = 1; i <= m; ++i) {
+        int64_t g;
+        border_cell(c, first_col_free, i, &H[i * W], &g);
+        P[i * W] = g; Q[i * W] = g;
+        for (uint64_t j = 1; j <= n; ++j) {
+            /* P(i,j), Q(i,j): the gap states entering (i,j); row 0 / column 0 hold H + goe */
+            const int64_t p = i == 1 ? H[j] + goe : max64(P[(i - 1) * W + j] + ext, H[(i - 1) * W + j] + goe);
+            const int64_t q = j == 1 ? H[i * W] + goe : max64(Q[i * W + j - 1] + ext, H[i * W + j - 1] + goe);
+            int64_t d = H[(i - 1) * W + j - 1] + substitute(c, s1[i - 1], s2[j - 1]);
+            if (local) d = max64(d, 0);
+            P[i * W + j] = p;
+            Q[i * W + j] = q;
+            H[i * W + j] = max64(max64(d, p), q);
+        }
+    }
+    /* walk back from the end cell; ops written in reverse, then flipped */
+    int64_t i = *end1, j = *end2, k = 0;
+    int state = 0;                                           /* 0 H, 1 P, 2 Q */
+    for (;;) {
+        if (state == 0) {
+            if (i == 0 || j == 0) {                          /* a border cell */
+                if (i == 0 && j > 0 && !first_row_free) { while (j > 0) { ops[k++] = 'I'; --j; } }
+                else if (j == 0 && i > 0 && !first_col_free) { while (i > 0) { ops[k++] = 'D'; --i; } }
+                break;
+            }
+            const int64_t h = H[i * W + j];
+            if (local && h == 0) break;
+            int64_t d = H[(i - 1) * W + j - 1] + substitute(c, s1[i - 1], s2[j - 1]);
+            if (local) d = max64(d, 0);
+            if (h == d) { ops[k++] = s1[i - 1] == s2[j - 1] ? '=' : 'X'; --i; --j; }
+            else if (h == P[i * W + j]) state = 1;
+            else state = 2;
+        } else if (state == 1) {                             /* P(i,j): 'D', to (i-1, j) */
+            const int64_t p = P[i * W + j];
+            ops[k++] = 'D';
+            const int ext_better = i > 1 && P[(i - 1) * W + j] + ext > H[(i - 1) * W + j] + goe;
+            (void)p;
+            --i;
+            state = ext_better ? 1 : 0;
+        } else {                                             /* Q(i,j): 'I', to (i, j-1) */
+            ops[k++] = 'I';
+            const int ext_better = j > 1 && Q[i * W + j - 1] + ext > H[i * W + j - 1] + goe;
+            --j;
+            state = ext_better ? 2 : 0;
+        }
+    }
+    *begin1 = i;
+    *begin2 = j;
+    for (int64_t a = 0, b = k - 1; a < b; ++a, --b) { uint8_t t = ops[a]; ops[a] = ops[b]; ops[b] = t; }
+    *n_ops = k;
+    free(H); free(P); free(Q);
+    return PA_ORACLE_OK;
+}
+
 /* H(row, 0..n) of the global recurrence (the scalar DP above stopped after
  * `row` rows of sequence1); out has n + 1 entries.  Used to check the band
  * labels: the label of checkpoint row r is argmax_j H(r, j) + H'(m - r, n - j)

@@ -7,8 +7,9 @@ and ``compute(...)`` results with ``score()``, computed by hand-written CUDA
 kernels through the C ABI of include/pairwise_aligner_gb300.h.
 """
 from . import cfg, seqio
-from .aligner import Aligner, AlignerResult, Context, RESULT_DTYPE, pack
+from .aligner import ALIGNMENT_DTYPE, Aligner, AlignerResult, AlignmentResult, Context, RESULT_DTYPE, cigar, pack
 from ._lib import PaError
 
-__all__ = ["cfg", "seqio", "Aligner", "AlignerResult", "Context", "RESULT_DTYPE", "pack", "PaError"]
+__all__ = ["cfg", "seqio", "Aligner", "AlignerResult", "AlignmentResult", "Context", "RESULT_DTYPE",
+           "ALIGNMENT_DTYPE", "cigar", "pack", "PaError"]
 __version__ = "0.1.0"

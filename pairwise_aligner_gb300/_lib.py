@@ -52,6 +52,15 @@ class PaResult(ctypes.Structure):
     ]
 
 
+class PaAlignment(ctypes.Structure):
+    _fields_ = [
+        ("begin1", ctypes.c_int32),
+        ("begin2", ctypes.c_int32),
+        ("n_ops", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+    ]
+
+
 class PaOptions(ctypes.Structure):
     _fields_ = [
         ("group_threads", ctypes.c_int32),
@@ -157,6 +166,9 @@ SIGNATURES = {
     "pa_align_batch_banded": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.POINTER(PaStats)], ctypes.c_int),
+    "pa_traceback_batch": ([_ctxp, ctypes.POINTER(PaConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                            ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                            ctypes.POINTER(PaStats)], ctypes.c_int),
     "pa_rank_map_device": ([_ctxp, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
                             ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "pa_pack_2bit_host": ([ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)],

@@ -152,6 +152,25 @@ RESULT_DTYPE = np.dtype([("score", np.int32), ("end1", np.int32), ("end2", np.in
 assert RESULT_DTYPE.itemsize == ctypes.sizeof(_lib.PaResult)
 
 
+ALIGNMENT_DTYPE = np.dtype([("begin1", np.int32), ("begin2", np.int32), ("n_ops", np.uint32), ("reserved", np.uint32)])
+assert ALIGNMENT_DTYPE.itemsize == ctypes.sizeof(_lib.PaAlignment)
+
+
+def cigar(ops: bytes) -> str:
+    """Run-length form of an op string ('=', 'X', 'I', 'D'), e.g. b'==XI' -> '2=1X1I'."""
+    out, prev, run = [], None, 0
+    for c in ops.decode() if isinstance(ops, (bytes, bytearray)) else ops:
+        if c == prev:
+            run += 1
+        else:
+            if prev is not None:
+                out.append(f"{run}{prev}")
+            prev, run = c, 1
+    if prev is not None:
+        out.append(f"{run}{prev}")
+    return "".join(out)
+
+
 class AlignerResult:
     """One alignment result (score only, plus the end position)."""
 
@@ -183,6 +202,31 @@ class AlignerResult:
 
     def __repr__(self):
         return f"AlignerResult(score={self._score}, end={self._end})"
+
+
+class AlignmentResult(AlignerResult):
+    """A result with its alignment (``Aligner.compute_traceback``)."""
+
+    __slots__ = ("_begin", "_ops")
+
+    def __init__(self, seq1, seq2, score, end1, end2, width, flags, begin1, begin2, ops):
+        super().__init__(seq1, seq2, score, end1, end2, width, flags)
+        self._begin = (int(begin1), int(begin2))
+        self._ops = bytes(ops)
+
+    def begin_position(self) -> tuple[int, int]:
+        """0-based cell the path starts after (symbols of sequence1 / sequence2 before it)."""
+        return self._begin
+
+    def ops(self) -> bytes:
+        """One byte per alignment column: '=', 'X', 'D' (sequence1 only), 'I' (sequence2 only)."""
+        return self._ops
+
+    def cigar(self) -> str:
+        return cigar(self._ops)
+
+    def __repr__(self):
+        return f"AlignmentResult(score={self._score}, begin={self._begin}, end={self._end}, cigar={self.cigar()!r})"
 
 
 class Aligner:
@@ -275,6 +319,40 @@ class Aligner:
         if stats:
             self.last_stats = self._stats_dict(st)
         return out[:n]
+
+    def compute_traceback_arrays(self, seq1: np.ndarray, off1: np.ndarray, seq2: np.ndarray, off2: np.ndarray):
+        """Host arrays in -> (results RESULT_DTYPE, alignments ALIGNMENT_DTYPE, ops uint8, ops offsets);
+        pair k's ops are ops[ops_off[k] : ops_off[k] + alignments[k]['n_ops']]."""
+        n = len(off1) - 1
+        if len(off2) - 1 != n:
+            raise ValueError("both sequence collections must hold the same number of sequences")
+        seq1 = np.ascontiguousarray(seq1, dtype=np.uint8)
+        seq2 = np.ascontiguousarray(seq2, dtype=np.uint8)
+        off1 = np.ascontiguousarray(off1, dtype=np.uint64)
+        off2 = np.ascontiguousarray(off2, dtype=np.uint64)
+        out = np.zeros(max(n, 1), dtype=RESULT_DTYPE)
+        aln = np.zeros(max(n, 1), dtype=ALIGNMENT_DTYPE)
+        ops_off = (off1 - off1[0]) + (off2 - off2[0]) if n else np.zeros(1, np.uint64)
+        ops = np.zeros(max(int(ops_off[-1]), 1), dtype=np.uint8)
+        st = _lib.PaStats()
+        ctx = self.context
+        cfg = self.c_config()
+        rc = ctx.lib.pa_traceback_batch(ctx.ptr, ctypes.byref(cfg), seq1.ctypes.data, off1.ctypes.data,
+                                        seq2.ctypes.data, off2.ctypes.data, n, out.ctypes.data, aln.ctypes.data,
+                                        ops.ctypes.data, ctypes.byref(st))
+        _lib.check(rc, ctx.ptr)
+        self.last_stats = self._stats_dict(st)
+        return out[:n], aln[:n], ops, ops_off[:n]
+
+    def compute_traceback(self, seqs1, seqs2) -> list:
+        """Like compute(seqs1, seqs2), with the alignment of every pair (AlignmentResult)."""
+        seqs1, seqs2 = list(seqs1), list(seqs2)
+        s1, o1 = pack(seqs1)
+        s2, o2 = pack(seqs2)
+        res, aln, ops, ops_off = self.compute_traceback_arrays(s1, o1, s2, o2)
+        return [AlignmentResult(a, b, r["score"], r["end1"], r["end2"], r["width"], r["flags"], g["begin1"],
+                                g["begin2"], ops[int(o):int(o) + int(g["n_ops"])].tobytes())
+                for a, b, r, g, o in zip(seqs1, seqs2, res, aln, ops_off)]
 
     def compute_banded(self, seq1: np.ndarray, off1: np.ndarray, seq2: np.ndarray, off2: np.ndarray,
                        bands: np.ndarray) -> np.ndarray:

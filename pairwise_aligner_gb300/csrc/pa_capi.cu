@@ -87,6 +87,8 @@ struct pa_ctx {
     int32_t mat_dim = 0, mat_max = 0, mat_min = 0;
     // input path: rank table, invalid-symbol counter, packed staging of pa_align_batch_packed
     DevBuf io_tab, io_ctr, in_words1, in_words2;
+    // traceback: direction words of one chunk, their per-pair offsets, alignments and ops
+    DevBuf tb_dir, tb_dir_off, tb_aln, tb_ops;
 };
 
 namespace {
@@ -1025,7 +1027,8 @@ pa_status pa_destroy(pa_ctx *c)
                       &c->band_spec, &c->band_win, &c->band_code, &c->band_bsum, &c->band_ctr, &c->band_in,
                       &c->mlp_feat, &c->mlp_x, &c->mlp_h1, &c->mlp_h2, &c->mlp_out,
                       &c->ring, &c->rerun_long, &c->mat_rank, &c->mat_scores,
-                      &c->io_tab, &c->io_ctr, &c->in_words1, &c->in_words2};
+                      &c->io_tab, &c->io_ctr, &c->in_words1, &c->in_words2,
+                      &c->tb_dir, &c->tb_dir_off, &c->tb_aln, &c->tb_ops};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     for (DevBuf &b : c->band_list)
@@ -1284,6 +1287,124 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
     PA_CUDA(ctx, cudaMemcpyAsync(out, ctx->in_out.p, n_pairs * sizeof(pa_result), cudaMemcpyDeviceToHost, st));
     PA_CUDA(ctx, cudaStreamSynchronize(st));
     return read_stats(ctx, stats);
+}
+
+// Traceback: inputs staged like pa_align_batch; pairs in chunks whose direction words fit
+// kTbBudgetWords; one kernel launch per chunk.
+constexpr uint64_t kTbBudgetWords = 1ull << 30;      // 4 GiB of direction words per chunk
+
+pa_status pa_traceback_batch(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1, const uint64_t *off1,
+                             const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, pa_result *out,
+                             pa_alignment *alignments, uint8_t *ops, pa_stats *stats)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    DpParams P;
+    ClassCfg C;
+    pa_status s = check_config(ctx, config, P, C);
+    if (s) return s;
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (n_pairs == 0) return PA_OK;
+    if (!seq1 || !off1 || !seq2 || !off2 || !out || !alignments || !ops)
+        return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null buffer");
+    if (n_pairs >= (1ull << 31)) return fail(ctx, PA_ERR_TOO_LARGE, "n_pairs must be < 2^31");
+    const bool use_matrix = C.rank_map != nullptr;
+    std::vector<uint64_t> words(n_pairs);
+    uint64_t cells = 0;
+    for (uint64_t k = 0; k < n_pairs; ++k) {
+        if (off1[k + 1] < off1[k] || off2[k + 1] < off2[k])
+            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "offsets must be non-decreasing");
+        const int64_t m = (int64_t)(off1[k + 1] - off1[k]), n = (int64_t)(off2[k + 1] - off2[k]);
+        if (m >= (1ll << 30) || n >= (1ll << 30)) return fail(ctx, PA_ERR_TOO_LARGE, "sequence longer than 2^30");
+        const int64_t a = std::abs((int64_t)P.match), b = std::abs((int64_t)P.mismatch);
+        const int64_t o = -(int64_t)P.gap_open, e = -(int64_t)P.gap_ext;
+        if ((a + b) * std::min(m, n) + (o + e) * (m + n + 2) + 2 * o >= (1ll << 30))
+            return fail(ctx, PA_ERR_OVERFLOW, "scores of some pairs could exceed int32");
+        words[k] = (m && n) ? (uint64_t)((n + kTracebackPassRows - 1) / kTracebackPassRows) * (m + 31) * 32 : 0;
+        if (words[k] > kTbBudgetWords) return fail(ctx, PA_ERR_TOO_LARGE, "a pair needs more than 4 GiB of directions");
+        cells += (uint64_t)(m * n);
+    }
+    if (use_matrix) {                                  // every symbol needs a rank
+        int8_t rank[256];
+        PA_CUDA(ctx, cudaMemcpy(rank, ctx->mat_rank.p, 256, cudaMemcpyDeviceToHost));
+        for (uint64_t x = off1[0]; x < off1[n_pairs]; ++x)
+            if (rank[seq1[x]] < 0) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "a symbol outside the substitution matrix");
+        for (uint64_t x = off2[0]; x < off2[n_pairs]; ++x)
+            if (rank[seq2[x]] < 0) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "a symbol outside the substitution matrix");
+    }
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, PA_ERR_CUDA, "cudaSetDevice");
+    const uint64_t base1 = off1[0], base2 = off2[0];
+    const uint64_t b1 = off1[n_pairs] - base1, b2 = off2[n_pairs] - base2;
+    if ((s = ensure(ctx, ctx->in_seq1, b1)) || (s = ensure(ctx, ctx->in_seq2, b2)) ||
+        (s = ensure(ctx, ctx->in_off1, (n_pairs + 1) * 8)) || (s = ensure(ctx, ctx->in_off2, (n_pairs + 1) * 8)) ||
+        (s = ensure(ctx, ctx->in_out, n_pairs * sizeof(pa_result))) ||
+        (s = ensure(ctx, ctx->boundary, (b1 + n_pairs) * sizeof(Cell))) ||
+        (s = ensure(ctx, ctx->tb_aln, n_pairs * sizeof(pa_alignment))) || (s = ensure(ctx, ctx->tb_ops, b1 + b2)) ||
+        (s = ensure(ctx, ctx->tb_dir_off, n_pairs * 8)))
+        return s;
+    std::vector<uint64_t> r1(off1, off1 + n_pairs + 1), r2(off2, off2 + n_pairs + 1);
+    for (auto &v : r1) v -= base1;
+    for (auto &v : r2) v -= base2;
+    cudaStream_t st = ctx->stream;
+    PA_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+    if (b1) PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_seq1.p, seq1 + base1, b1, cudaMemcpyHostToDevice, st));
+    if (b2) PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_seq2.p, seq2 + base2, b2, cudaMemcpyHostToDevice, st));
+    PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off1.p, r1.data(), (n_pairs + 1) * 8, cudaMemcpyHostToDevice, st));
+    PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off2.p, r2.data(), (n_pairs + 1) * 8, cudaMemcpyHostToDevice, st));
+    // chunks: consecutive pairs whose direction words fit the budget
+    std::vector<uint64_t> dir_off(n_pairs);
+    TbLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.seq1 = (const uint8_t *)ctx->in_seq1.p;
+    L.seq2 = (const uint8_t *)ctx->in_seq2.p;
+    L.off1 = (const uint64_t *)ctx->in_off1.p;
+    L.off2 = (const uint64_t *)ctx->in_off2.p;
+    L.bnd = (Cell *)ctx->boundary.p;
+    L.out = (pa_result *)ctx->in_out.p;
+    L.aln = (pa_alignment *)ctx->tb_aln.p;
+    L.ops = (uint8_t *)ctx->tb_ops.p;
+    if (use_matrix) {
+        L.rank = (const int8_t *)ctx->mat_rank.p;
+        L.matrix = (const int32_t *)ctx->mat_scores.p;
+        L.dim = ctx->mat_dim;
+    }
+    const int grid = traceback_grid(ctx->sm_count);
+    uint64_t launches = 0;
+    for (uint64_t first = 0; first < n_pairs;) {
+        uint64_t total = 0, end = first;
+        while (end < n_pairs && total + words[end] <= kTbBudgetWords) {
+            dir_off[end - first] = total;
+            total += words[end];
+            ++end;
+        }
+        if ((s = ensure(ctx, ctx->tb_dir, std::max<uint64_t>(total, 1) * 4))) return s;
+        // the previous chunk's kernel may still read the offsets: copy them in stream order
+        PA_CUDA(ctx, cudaMemcpyAsync(ctx->tb_dir_off.p, dir_off.data(), (end - first) * 8, cudaMemcpyHostToDevice, st));
+        PA_CUDA(ctx, cudaStreamSynchronize(st));        // dir_off is reused by the next chunk
+        L.first = (uint32_t)first;
+        L.count = (uint32_t)(end - first);
+        L.dir_off = (const uint64_t *)ctx->tb_dir_off.p;
+        L.dir = (uint32_t *)ctx->tb_dir.p;
+        traceback_launch(grid, st, L, P);
+        ++launches;
+        first = end;
+    }
+    PA_CUDA(ctx, cudaGetLastError());
+    PA_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+    PA_CUDA(ctx, cudaMemcpyAsync(out, ctx->in_out.p, n_pairs * sizeof(pa_result), cudaMemcpyDeviceToHost, st));
+    PA_CUDA(ctx, cudaMemcpyAsync(alignments, ctx->tb_aln.p, n_pairs * sizeof(pa_alignment), cudaMemcpyDeviceToHost, st));
+    if (b1 + b2) PA_CUDA(ctx, cudaMemcpyAsync(ops, ctx->tb_ops.p, b1 + b2, cudaMemcpyDeviceToHost, st));
+    PA_CUDA(ctx, cudaStreamSynchronize(st));
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        stats->pairs = n_pairs;
+        stats->cells = cells;
+        stats->pairs_s32 = n_pairs;
+        stats->kernel_launches = launches;
+        stats->device_ms = ms;
+        stats->dp_ms = ms;
+    }
+    return PA_OK;
 }
 
 pa_status pa_align_batch_packed(pa_ctx *ctx, const pa_config *config, const uint32_t *seq1_words,

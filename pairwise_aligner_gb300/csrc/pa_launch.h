@@ -24,4 +24,24 @@ int dp_cluster_grid(bool lanes16, bool gen, int mode, int max_blocks);
 cudaError_t dp_cluster_launch(bool lanes16, bool gen, int mode, int grid, cudaStream_t stream, const DpLaunch &L,
                               const DpParams &P);
 
+// Traceback (pa_traceback.cu): one warp per pair, direction words of pair q at dir + dir_off[q],
+// passes * (m + 31) * 32 words with passes = ceil(n / kTracebackPassRows).
+constexpr int kTracebackPassRows = 256;
+struct TbLaunch {
+    const uint8_t *seq1, *seq2;
+    const uint64_t *off1, *off2;
+    uint32_t first, count;          // the chunk: pairs first .. first + count - 1
+    const uint64_t *dir_off;        // per chunk pair: first direction word
+    uint32_t *dir;
+    Cell *bnd;                      // pass boundary: (H(i, last row of the pass), Q(i, next row))
+    pa_result *out;
+    pa_alignment *aln;
+    uint8_t *ops;                   // pair k at (off1[k] - off1[0]) + (off2[k] - off2[0]), m + n bytes
+    const int8_t *rank;             // substitution matrix (or null: match / mismatch)
+    const int32_t *matrix;
+    int32_t dim;
+};
+int traceback_grid(int sm_count);
+void traceback_launch(int grid, cudaStream_t stream, const TbLaunch &L, const DpParams &P);
+
 }  // namespace pa
