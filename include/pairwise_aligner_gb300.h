@@ -220,7 +220,7 @@ pa_status pa_mlp_to_bf16(const float *src, int rows, int cols, int ld_dst, void 
 
 /* Pairs with at least `cells` = m * n cells are computed by whole thread blocks
  * (the warps of a block pipeline the pair's row passes) instead of one group of
- * lanes; default 2^22.  1 sends every pair there, UINT64_MAX none. */
+ * lanes; default 2^20.  1 sends every pair there, UINT64_MAX none. */
 pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells);
 
 /* Of those, pairs with at least `cells` cells and `min_rows` rows of sequence2 are

@@ -64,7 +64,7 @@ struct pa_ctx {
     DevBuf ring, rerun_long;      // CTA mode: boundary rows per block; s16 long pairs to redo in s32
     int32_t ring_m = 0;           // longest sequence1 the ring rows hold (0: no CTA mode yet)
     int ring_grid = 0;            // blocks of every CTA-mode launch
-    int64_t long_cells = 1ll << 22;   // pairs with at least this many cells use CTA mode
+    int64_t long_cells = 1ll << 20;   // pairs with at least this many cells use CTA mode
     int64_t huge_cells = 1ll << 28;   // ... and with this many (and n >= huge_min_n) cluster mode
     int32_t huge_min_n = 8192;
     int64_t want_ring_m = 0;          // the next call's longest CTA-mode sequence1 (host: exact)
