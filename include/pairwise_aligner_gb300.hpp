@@ -20,6 +20,7 @@
 // reference's only runtime error does (tracker_global_simd_saturated.hpp:98-100).
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <concepts>
 #include <cstddef>
@@ -208,6 +209,34 @@ private:
     pa_result _r;
 };
 
+// A result with its alignment (aligner::compute_alignments): the 0-based cell the path starts
+// after and one op per alignment column ('=', 'X', 'D': a sequence1 symbol against a gap,
+// 'I': a sequence2 symbol against a gap).
+class alignment_result : public aligner_result {
+public:
+    alignment_result(aligner_result base, pa_alignment a, std::string ops)
+        : aligner_result{std::move(base)}, _a{a}, _ops{std::move(ops)}
+    {}
+    std::pair<int32_t, int32_t> begin_position() const noexcept { return {_a.begin1, _a.begin2}; }
+    std::string_view ops() const noexcept { return _ops; }
+    std::string cigar() const
+    {
+        std::string out;
+        for (size_t k = 0; k < _ops.size();) {
+            size_t e = k;
+            while (e < _ops.size() && _ops[e] == _ops[k]) ++e;
+            out += std::to_string(e - k);
+            out += _ops[k];
+            k = e;
+        }
+        return out;
+    }
+
+private:
+    pa_alignment _a;
+    std::string _ops;
+};
+
 class aligner {
 public:
     explicit aligner(cfg::settings const &s, int device = 0)
@@ -253,6 +282,30 @@ public:
         res.reserve(n);
         for (uint64_t k = 0; k < n; ++k)
             res.emplace_back(s1, s2, o1[k], o1[k + 1] - o1[k], o2[k], o2[k + 1] - o2[k], out[k]);
+        return res;
+    }
+
+    // Bulk with alignments (pa_traceback_batch): the same results plus begin cell and ops.
+    template <std::ranges::forward_range seqs1_t, std::ranges::forward_range seqs2_t>
+        requires std::ranges::forward_range<std::ranges::range_reference_t<seqs1_t>>
+    std::vector<alignment_result> compute_alignments(seqs1_t &&seqs1, seqs2_t &&seqs2)
+    {
+        auto [s1, o1] = pack(seqs1);
+        auto [s2, o2] = pack(seqs2);
+        if (o1.size() != o2.size()) throw std::runtime_error("both collections must hold the same number of sequences");
+        const uint64_t n = o1.size() - 1;
+        std::vector<pa_result> out(n);
+        std::vector<pa_alignment> aln(n);
+        std::string ops(std::max<uint64_t>(o1.back() + o2.back(), 1), '\0');
+        check(pa_traceback_batch(_ctx.get(), &_cfg, reinterpret_cast<const uint8_t *>(s1->data()), o1.data(),
+                                 reinterpret_cast<const uint8_t *>(s2->data()), o2.data(), n, out.data(), aln.data(),
+                                 reinterpret_cast<uint8_t *>(ops.data()), nullptr),
+              _ctx.get());
+        std::vector<alignment_result> res;
+        res.reserve(n);
+        for (uint64_t k = 0; k < n; ++k)
+            res.emplace_back(aligner_result{s1, s2, o1[k], o1[k + 1] - o1[k], o2[k], o2[k + 1] - o2[k], out[k]}, aln[k],
+                             ops.substr(o1[k] + o2[k], aln[k].n_ops));
         return res;
     }
 

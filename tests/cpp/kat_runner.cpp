@@ -2,7 +2,9 @@
 // with the reference's rule nesting.  stdin: one case per line,
 //   method open ext match mismatch first_column first_row last_column last_row seq1 seq2
 // (method 0 global / 1 local, end-gap flags 0 penalised / 1 free, "-" = empty sequence).
-// A line starting with "M" scores with a substitution matrix (cfg::score_model_matrix):
+// A line starting with "T" prints the global alignment (compute_alignments) as
+//   "score begin1 begin2 end1 end2 cigar";
+// a line starting with "M" scores with a substitution matrix (cfg::score_model_matrix):
 //   M method open ext first_column first_row last_column last_row dim symbols s_0 .. s_{dim*dim-1} seq1 seq2
 // stdout: "score end1 end2" per case, all cases of one configuration aligned in one bulk call.
 #include <array>
@@ -53,6 +55,25 @@ int main()
     while (std::getline(std::cin, line)) {
         if (line.empty()) continue;
         std::istringstream in{line};
+        if (line[0] == 'T') {                          // T match mismatch open ext seq1 seq2: global alignment
+            std::string tag, a, b;
+            int match, mismatch, open, ext;
+            in >> tag >> match >> mismatch >> open >> ext >> a >> b;
+            if (a == "-") a.clear();
+            if (b == "-") b.clear();
+            try {
+                auto al = aligner::cfg::configure_aligner(aligner::cfg::score_model_unitary(
+                    aligner::cfg::method_global(aligner::cfg::gap_model_affine(open, ext)), match, mismatch));
+                std::vector<std::string> s1{a}, s2{b};
+                auto r = al.compute_alignments(s1, s2).front();
+                std::cout << r.score() << ' ' << r.begin_position().first << ' ' << r.begin_position().second << ' '
+                          << r.end_position().first << ' ' << r.end_position().second << ' '
+                          << (r.cigar().empty() ? "-" : r.cigar()) << '\n';
+            } catch (std::exception const &ex) {
+                std::cout << "error " << ex.what() << '\n';
+            }
+            continue;
+        }
         if (line[0] == 'M') {
             std::string tag;
             int method, open, ext, fc, fr, lc, lr, dim;

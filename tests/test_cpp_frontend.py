@@ -57,6 +57,24 @@ def test_cpp_frontend_matrix_kats(runner, matrix_kats):
 
 
 @pytest.mark.gpu
+def test_cpp_frontend_alignments(runner, oracle):
+    """compute_alignments through the C++ rule chain equals the oracle's traceback."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pairwise_aligner_gb300 import cigar
+    cases = [("ACGTACGT", "ACGTTACGT"), ("ACGT", "AGT"), ("-", "ACG"), ("GATTACA", "GCATGCT"), ("AAAA", "-")]
+    lines = [f"T 2 -3 -5 -1 {a} {b}" for a, b in cases]
+    out = subprocess.run([runner], input="\n".join(lines) + "\n", capture_output=True, text=True,
+                         check=True).stdout.split("\n")
+    cfg = oracle.make_cfg(2, -3, -5, -1)
+    for (a, b), line in zip(cases, out):
+        a, b = a.replace("-", ""), b.replace("-", "")
+        sc, b1, b2, e1, e2, ops = oracle.traceback(cfg, a.encode(), b.encode())
+        assert line.split() == [str(sc), str(b1), str(b2), str(e1), str(e2), cigar(ops) or "-"], (a, b, line)
+
+
+@pytest.mark.gpu
 def test_cpp_frontend_reference_kats(runner, kats):
     import torch
     if not torch.cuda.is_available():
