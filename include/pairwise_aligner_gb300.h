@@ -223,6 +223,11 @@ pa_status pa_mlp_to_bf16(const float *src, int rows, int cols, int ld_dst, void 
  * lanes; default 2^20.  1 sends every pair there, UINT64_MAX none. */
 pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells);
 
+/* Of those, pairs whose sequence2 has at most `max_rows` rows (few 512-row passes) run on
+ * teams of 4 warps, two pairs per block, instead of all 8 warps of a block; default
+ * 4096 (8 passes), 0 keeps every such pair on whole blocks. */
+pa_status pa_set_team_threshold(pa_ctx *ctx, uint32_t max_rows);
+
 /* Of those, pairs with at least `cells` cells and `min_rows` rows of sequence2 are
  * computed by clusters of 4 thread blocks (co-scheduled; their 32 warps pipeline the
  * pair's passes); defaults 2^28 and 8192. */

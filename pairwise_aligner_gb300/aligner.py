@@ -69,6 +69,10 @@ class Context:
         """Of the block-mode pairs, those with at least `cells` cells and `min_rows` rows run on clusters."""
         _lib.check(self.lib.pa_set_cluster_threshold(self.ptr, int(cells), int(min_rows)), self.ptr)
 
+    def set_team_threshold(self, max_rows: int):
+        """Block-mode pairs whose sequence2 has at most `max_rows` rows run on 4-warp teams (0: none)."""
+        _lib.check(self.lib.pa_set_team_threshold(self.ptr, int(max_rows)), self.ptr)
+
     def set_substitution_matrix(self, symbols: bytes, scores):
         """Load the matrix that PA_SCORE_MATRIX calls score with: scores[r1 * dim + r2] for a
         sequence1 symbol of rank r1 (its index in `symbols`) against a sequence2 symbol of rank r2."""

@@ -67,6 +67,7 @@ struct pa_ctx {
     int64_t long_cells = 1ll << 20;   // pairs with at least this many cells use CTA mode
     int64_t huge_cells = 1ll << 28;   // ... and with this many (and n >= huge_min_n) cluster mode
     int32_t huge_min_n = 8192;
+    int32_t team_max_n = 4096;        // CTA-mode pairs with at most this many rows run on 4-warp teams
     int64_t want_ring_m = 0;          // the next call's longest CTA-mode sequence1 (host: exact)
     DevBuf in_seq1, in_off1, in_seq2, in_off2, in_out;   // staging for the host-buffer entry points
     int G[3] = {kDefaultG, kDefaultG, kDefaultG};
@@ -184,6 +185,7 @@ pa_status check_config(pa_ctx *c, const pa_config *cfg, DpParams &P, ClassCfg &C
     C.long_cells = c->long_cells;
     C.huge_cells = c->huge_cells;
     C.huge_min_n = c->huge_min_n;
+    C.team_max_n = c->team_max_n;
     C.long_max_m = c->ring.p ? c->ring_m : 0;
     return PA_OK;
 }
@@ -400,6 +402,12 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
         LL.lead_order = nullptr;
         LL.lead_begin_ptr = nullptr;
         LL.lead_count_ptr = nullptr;
+        // long pairs with few passes: teams of 4 warps, after the blocks' longer pairs
+        const Klass mc[3] = {K_S16M, K_S32M, K_GENM};
+        for (int k = 0; k < 3 && C.team_max_n > 0; ++k) {
+            LL.begin_ptr = ranges + mc[k]; LL.count_ptr = counts + mc[k]; LL.unit_counter = counters + 22 + k;
+            dp_team_launch(k == 0, k == 2, mode, c->ring_grid, st, LL, P);
+        }
         PA_CUDA(c, cudaStreamWaitEvent(st, c->ev_join, 0));   // the cluster kernels' results and redo list
         if (mode != M_LOCAL) {
             LL.order = (const uint32_t *)c->rerun_long.p;
@@ -409,7 +417,7 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
             LL.rerun = 1;
             dp_cta_launch(false, false, mode, c->ring_grid, st, LL, P);
         }
-        c->last_launches += mode != M_LOCAL ? 7 : 6;
+        c->last_launches += (mode != M_LOCAL ? 7 : 6) + (C.team_max_n > 0 ? 3 : 0);
     }
     // s16 global results that failed the exactness check, recomputed in s32
     if (mode != M_LOCAL) {
@@ -438,6 +446,9 @@ pa_status ensure_ring(pa_ctx *c, int64_t max_m)
         per_sm = std::max(per_sm, dp_cta_occupancy(true, false, mode));
         per_sm = std::max(per_sm, dp_cta_occupancy(false, false, mode));
         per_sm = std::max(per_sm, dp_cta_occupancy(false, true, mode));
+        per_sm = std::max(per_sm, dp_team_occupancy(true, false, mode));
+        per_sm = std::max(per_sm, dp_team_occupancy(false, false, mode));
+        per_sm = std::max(per_sm, dp_team_occupancy(false, true, mode));
     }
     per_sm = std::max(per_sm, band_cta_occupancy());
     per_sm = std::max(per_sm, band_labels_cta_occupancy());
@@ -534,6 +545,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     DpParams P;
     ClassCfg C;
     if ((s = check_config(c, cfg, P, C))) return s;
+    C.team_max_n = 0;                                 // band mode has its own team choice
     if (P.local || P.first_column_free || P.first_row_free || P.last_column_free || P.last_row_free)
         return fail(c, PA_ERR_UNSUPPORTED, "band mode needs global alignment with penalised end gaps");
     if (!h_bands && cfg->band_mode == 1 && !c->has_model)
@@ -830,9 +842,9 @@ pa_status read_stats(pa_ctx *c, pa_stats *stats)
         cudaGetLastError();
         const uint64_t rr = (uint64_t)ctr[4] + ctr[6];
         stats->cells = ps.cells;
-        stats->pairs_s16 = ps.n_class[K_S16] + ps.n_class[K_S16L] + ps.n_class[K_S16H] - rr;
-        stats->pairs_s32 = ps.n_class[K_S32] + ps.n_class[K_S32L] + ps.n_class[K_S32H] + rr;
-        stats->pairs_general = ps.n_class[K_GEN] + ps.n_class[K_GENL] + ps.n_class[K_GENH];
+        stats->pairs_s16 = ps.n_class[K_S16] + ps.n_class[K_S16L] + ps.n_class[K_S16H] + ps.n_class[K_S16M] - rr;
+        stats->pairs_s32 = ps.n_class[K_S32] + ps.n_class[K_S32L] + ps.n_class[K_S32H] + ps.n_class[K_S32M] + rr;
+        stats->pairs_general = ps.n_class[K_GEN] + ps.n_class[K_GENL] + ps.n_class[K_GENH] + ps.n_class[K_GENM];
         stats->pairs_trivial = ps.n_class[K_NONE];
         stats->pairs_rerun = rr;
     }
@@ -1103,6 +1115,15 @@ pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells)
     if (!ctx) return PA_ERR_INVALID_ARGUMENT;
     ctx->long_cells = cells > (uint64_t)INT64_MAX ? INT64_MAX : (int64_t)std::max<uint64_t>(cells, 1);
     for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);   // the classifier's rule changed
+    ctx->graphs.clear();
+    return PA_OK;
+}
+
+pa_status pa_set_team_threshold(pa_ctx *ctx, uint32_t max_rows)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    ctx->team_max_n = (int32_t)std::min<uint32_t>(max_rows, 1u << 30);
+    for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
     ctx->graphs.clear();
     return PA_OK;
 }

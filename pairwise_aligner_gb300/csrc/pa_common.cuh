@@ -21,14 +21,16 @@ struct DpParams {
 
 // Work classes produced by the classifier; the class is the top field of the bucket key.
 // Classes 4..6 are the long-pair versions of 0..2, computed by whole blocks (CTA mode);
-// 8..10 the largest pairs, computed by thread-block clusters (cluster mode).
+// 8..10 the largest pairs, computed by thread-block clusters (cluster mode); 12..14 long
+// pairs with few row passes, computed by teams of 4 warps (two pairs per block).
 enum Klass : uint32_t {
     K_S16 = 0, K_S32 = 1, K_GEN = 2, K_NONE = 3, K_S16L = 4, K_S32L = 5, K_GENL = 6,
-    K_S16H = 8, K_S32H = 9, K_GENH = 10
+    K_S16H = 8, K_S32H = 9, K_GENH = 10, K_S16M = 12, K_S32M = 13, K_GENM = 14
 };
-constexpr int kClasses = 11;
+constexpr int kClasses = 15;
 constexpr uint32_t kLongOffset = 4;
 constexpr uint32_t kHugeOffset = 8;
+constexpr uint32_t kMediumOffset = 12;      // block-mode pairs with few passes: teams of 4 warps
 constexpr int kClusterBlocks = 4;            // blocks per cluster in cluster mode
 
 constexpr int kKeyBits = 20;                 // 4 class | 6 pass | 10 length bits

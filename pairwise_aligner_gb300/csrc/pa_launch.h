@@ -17,6 +17,10 @@ void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStre
 int dp_cta_occupancy(bool lanes16, bool gen, int mode);
 void dp_cta_launch(bool lanes16, bool gen, int mode, int grid, cudaStream_t stream, const DpLaunch &L,
                    const DpParams &P);
+// The same pairs on teams of 4 warps (two units per block, same ring rows as CTA mode).
+int dp_team_occupancy(bool lanes16, bool gen, int mode);
+void dp_team_launch(bool lanes16, bool gen, int mode, int grid, cudaStream_t stream, const DpLaunch &L,
+                    const DpParams &P);
 
 // Cluster mode (the largest pairs): clusters of kClusterBlocks blocks per pair; the grid is a
 // multiple of the cluster size and L.ring holds grid * 8 rows.  mode may be M_BAND.

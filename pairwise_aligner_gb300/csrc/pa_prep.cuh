@@ -21,6 +21,7 @@ struct ClassCfg {
     int64_t huge_cells;      // ... and with m*n at least this and n >= huge_min_n to cluster mode
     int32_t long_max_m;      // the longest sequence1 the ring rows hold
     int32_t huge_min_n;
+    int32_t team_max_n;      // CTA-mode pairs with n at most this run on teams of 4 warps (0: none)
     const int8_t *rank_map;  // substitution-matrix scoring: symbol -> rank (null: unitary scores)
 };
 
@@ -115,9 +116,11 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
         else if (!C.force32 && C.s16_params && (!C.local || (int64_t)P.smax * min(m, n) <= 30000)) klass = K_S16;
         else klass = K_S32;
         if (klass != K_NONE && m * n >= C.long_cells && m <= C.long_max_m && n <= (1 << 20))
-            klass += (m * n >= C.huge_cells && n >= C.huge_min_n) ? kHugeOffset : kLongOffset;
+            klass += (m * n >= C.huge_cells && n >= C.huge_min_n) ? kHugeOffset
+                     : (n <= C.team_max_n)                        ? kMediumOffset
+                                                                  : kLongOffset;
         if (klass == K_S16 || klass == K_S32 || klass == K_S16L || klass == K_S32L || klass == K_S16H ||
-            klass == K_S32H) {
+            klass == K_S32H || klass == K_S16M || klass == K_S32M) {
             uint32_t *qt = qtab + q0 + p;
             for (int64_t i = 4 * lane; i <= m; i += 128) {
                 const uint8_t *a = seq1 + q0 + i;

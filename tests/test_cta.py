@@ -212,3 +212,29 @@ def test_band_teams_of_warps_exact(pa, oracle):
         al = pa.Aligner(dict(c, band_mode=2), context=ctx)
         res = al.compute_arrays(q, qo, t, to)
         _check(oracle, c, q, qo, t, to, res)
+
+
+@pytest.mark.parametrize("c", [_cfg(), _cfg(local=True, match=1, mismatch=-4, gap_open=-6),
+                               _cfg(last_row_free=True, last_column_free=True),
+                               _cfg(first_column_free=True, last_row_free=True)])
+def test_team_class_forced(pa, oracle, c):
+    """Block-mode pairs with few passes on 4-warp teams (the medium class), forced on short pairs."""
+    q, qo, t, to = _pairs(11, SHORT * 3)
+    for team_rows in (1 << 30, 600):
+        ctx = pa.Context(0)
+        ctx.set_cta_threshold(1)
+        ctx.set_team_threshold(team_rows)
+        res = pa.Aligner(c, context=ctx).compute_arrays(q, qo, t, to)
+        _check(oracle, c, q, qo, t, to, res)
+
+
+def test_team_class_long_pairs_and_redo(pa, oracle):
+    """Default block threshold, teams for n <= 4096, byte-compare pairs and s16 -> s32 redo among them."""
+    q, qo, t, to = _pairs(12, [(2500, 2400), (3000, 3900), (2100, 5000), (4000, 1200)] * 2, unrelated=True)
+    t = t.copy()
+    t[50] = ord("N")
+    for c in (_cfg(gap_open=-5, gap_extension=-2), _cfg(local=True, match=1, mismatch=-4, gap_open=-6)):
+        ctx = pa.Context(0)
+        ctx.set_team_threshold(4096)
+        res = pa.Aligner(c, context=ctx).compute_arrays(q, qo, t, to)
+        _check(oracle, c, q, qo, t, to, res)
