@@ -896,7 +896,7 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
             if (ce != cudaSuccess) return fail(c, PA_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ce));
             it = c->graphs.emplace(key, ex).first;
         } else {
-            c->last_launches = 6 + 3 + (P.local ? 0 : 1) + (c->ring.p ? (P.local ? 7 : 8) : 0);
+            c->last_launches = 6 + 3 + (P.local ? 0 : 1) + (c->ring.p ? (P.local ? 7 : 8) + (C.team_max_n > 0 ? 3 : 0) : 0);
         }
         PA_CUDA(c, cudaGraphLaunch(it->second, c->stream));
     } else {
