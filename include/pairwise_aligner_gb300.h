@@ -224,8 +224,9 @@ pa_status pa_mlp_to_bf16(const float *src, int rows, int cols, int ld_dst, void 
 pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells);
 
 /* Of those, pairs whose sequence2 has at most `max_rows` rows (few 512-row passes) run on
- * teams of 4 warps, two pairs per block, instead of all 8 warps of a block; default
- * 4096 (8 passes), 0 keeps every such pair on whole blocks. */
+ * teams of 4 warps, two pairs per block, instead of all 8 warps of a block (beside
+ * them, on the SMs their blocks release); default 8192 (16 passes), 0 keeps every
+ * such pair on whole blocks. */
 pa_status pa_set_team_threshold(pa_ctx *ctx, uint32_t max_rows);
 
 /* Of those, pairs with at least `cells` cells and `min_rows` rows of sequence2 are

@@ -57,6 +57,8 @@ struct pa_ctx {
     cudaEvent_t ev_dp0 = nullptr, ev_dp1 = nullptr;   // bracket the DP kernels of the last call
     cudaStream_t side = nullptr;                      // cluster-mode kernels run beside the others
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t side2 = nullptr;                     // team kernels run beside the CTA kernels
+    cudaEvent_t ev_join2 = nullptr;
     pa_options opt{};
     std::string err;
     // device work buffers (grow only)
@@ -67,7 +69,7 @@ struct pa_ctx {
     int64_t long_cells = 1ll << 20;   // pairs with at least this many cells use CTA mode
     int64_t huge_cells = 1ll << 28;   // ... and with this many (and n >= huge_min_n) cluster mode
     int32_t huge_min_n = 8192;
-    int32_t team_max_n = 4096;        // CTA-mode pairs with at most this many rows run on 4-warp teams
+    int32_t team_max_n = 8192;        // CTA-mode pairs with at most this many rows run on 4-warp teams
     int64_t want_ring_m = 0;          // the next call's longest CTA-mode sequence1 (host: exact)
     DevBuf in_seq1, in_off1, in_seq2, in_off2, in_out;   // staging for the host-buffer entry points
     int G[3] = {kDefaultG, kDefaultG, kDefaultG};
@@ -95,6 +97,11 @@ struct pa_ctx {
 namespace {
 
 // The ring rows of cluster-mode launches (CTA-mode launches use the first region).
+Cell *team_ring(pa_ctx *c)
+{
+    return (Cell *)c->ring.p + (size_t)2 * c->ring_grid * 8 * ((size_t)c->ring_m + 2);
+}
+
 Cell *cluster_ring(pa_ctx *c)
 {
     return (Cell *)c->ring.p + (size_t)c->ring_grid * 8 * ((size_t)c->ring_m + 2);
@@ -402,11 +409,20 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
         LL.lead_order = nullptr;
         LL.lead_begin_ptr = nullptr;
         LL.lead_count_ptr = nullptr;
-        // long pairs with few passes: teams of 4 warps, after the blocks' longer pairs
-        const Klass mc[3] = {K_S16M, K_S32M, K_GENM};
-        for (int k = 0; k < 3 && C.team_max_n > 0; ++k) {
-            LL.begin_ptr = ranges + mc[k]; LL.count_ptr = counts + mc[k]; LL.unit_counter = counters + 22 + k;
-            dp_team_launch(k == 0, k == 2, mode, c->ring_grid, st, LL, P);
+        // long pairs with few passes: teams of 4 warps on a second side stream with their own
+        // ring rows, launched after the CTA-mode kernels so that those take the SMs first; the
+        // teams fill the SMs that the blocks of the longer pairs release
+        if (C.team_max_n > 0) {
+            PA_CUDA(c, cudaStreamWaitEvent(c->side2, c->ev_fork, 0));
+            DpLaunch LT = LL;
+            LT.ring = team_ring(c);
+            const Klass mc[3] = {K_S16M, K_S32M, K_GENM};
+            for (int k = 0; k < 3; ++k) {
+                LT.begin_ptr = ranges + mc[k]; LT.count_ptr = counts + mc[k]; LT.unit_counter = counters + 22 + k;
+                dp_team_launch(k == 0, k == 2, mode, c->ring_grid, c->side2, LT, P);
+            }
+            PA_CUDA(c, cudaEventRecord(c->ev_join2, c->side2));
+            PA_CUDA(c, cudaStreamWaitEvent(st, c->ev_join2, 0));   // the team kernels' results and redo list
         }
         PA_CUDA(c, cudaStreamWaitEvent(st, c->ev_join, 0));   // the cluster kernels' results and redo list
         if (mode != M_LOCAL) {
@@ -455,7 +471,8 @@ pa_status ensure_ring(pa_ctx *c, int64_t max_m)
     const int grid = per_sm * c->sm_count;
     const int32_t m = (int32_t)std::max<int64_t>(max_m, c->ring_m);
     // two regions: CTA-mode blocks and cluster-mode blocks run at the same time
-    pa_status s = ensure(c, c->ring, (size_t)2 * grid * 8 * ((size_t)m + 2) * sizeof(Cell));
+    // three regions: CTA-mode blocks, cluster-mode blocks and team blocks run at the same time
+    pa_status s = ensure(c, c->ring, (size_t)3 * grid * 8 * ((size_t)m + 2) * sizeof(Cell));
     if (s) return s;
     c->ring_m = m;
     c->ring_grid = grid;
@@ -1001,6 +1018,8 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
         cudaEventCreate(&c->ev2) != cudaSuccess || cudaEventCreate(&c->ev3) != cudaSuccess ||
         cudaEventCreate(&c->ev_dp0) != cudaSuccess || cudaEventCreate(&c->ev_dp1) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
@@ -1056,6 +1075,8 @@ pa_status pa_destroy(pa_ctx *c)
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->side2) cudaStreamDestroy(c->side2);
+    if (c->ev_join2) cudaEventDestroy(c->ev_join2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return PA_OK;
