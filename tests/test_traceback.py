@@ -188,3 +188,43 @@ def test_traceback_reference_kats_through_rules(pa, kats, oracle):
             cfg = oracle_cfg_of(oracle, c)
             b1, b2 = r.begin_position()
             assert oracle.rescore(cfg, c["seq1"].encode(), c["seq2"].encode(), b1, b2, r.ops()) == r.score()
+
+
+def _all_alignments(a: bytes, b: bytes):
+    """Every op string aligning all of a with all of b (small inputs only)."""
+    if not a and not b:
+        yield ""
+        return
+    if a and b:
+        for rest in _all_alignments(a[1:], b[1:]):
+            yield ("=" if a[0] == b[0] else "X") + rest
+    if a:
+        for rest in _all_alignments(a[1:], b):
+            yield "D" + rest
+    if b:
+        for rest in _all_alignments(a, b[1:]):
+            yield "I" + rest
+
+
+def test_oracle_traceback_is_optimal_by_enumeration(oracle):
+    """Global (penalised ends) and local paths against the best of all alignments, enumerated."""
+    rng = np.random.default_rng(21)
+    for match, mismatch, go, ge in ((2, -3, -5, -1), (1, -1, 0, -1), (3, -2, -4, -2)):
+        g = oracle.make_cfg(match, mismatch, go, ge)
+        lo = oracle.make_cfg(match, mismatch, go, ge, local=True)
+        for _ in range(25):
+            a = ACGT[rng.integers(0, 4, int(rng.integers(0, 5)))].tobytes()
+            b = ACGT[rng.integers(0, 4, int(rng.integers(0, 5)))].tobytes()
+            best = max(oracle.rescore(g, a, b, 0, 0, ops.encode()) for ops in _all_alignments(a, b))
+            sc, b1, b2, e1, e2, ops = oracle.traceback(g, a, b)
+            assert sc == best and (b1, b2, e1, e2) == (0, 0, len(a), len(b))
+            assert oracle.rescore(g, a, b, 0, 0, ops) == best
+            if a and b:                                 # local: the best over all substring pairs
+                lbest = max(oracle.rescore(lo, a[i:k], b[j:l], 0, 0, ops.encode())
+                            for i in range(len(a)) for k in range(i + 1, len(a) + 1)
+                            for j in range(len(b)) for l in range(j + 1, len(b) + 1)
+                            for ops in _all_alignments(a[i:k], b[j:l]))
+                sc, b1, b2, e1, e2, ops = oracle.traceback(lo, a, b)
+                assert sc == max(lbest, 0)
+                if sc > 0:
+                    assert oracle.rescore(lo, a, b, b1, b2, ops) == sc
