@@ -438,7 +438,7 @@ def input_kernels(dev, stream, ctx, n: int = 1 << 30, reps: int = 5) -> dict:
 
 
 def max_over_ranks(x: float, world: int) -> float:
-    """The slowest rank's value (times are maxed over ranks, like the driver's clock)."""
+    """The slowest rank's value: a job's time is its slowest rank's."""
     if world <= 1:
         return x
     import torch

@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Regenerate the golden fixtures in tests/golden/ from the reference's own tests.
 
-Runs only where the reference checkout is present (this build container); the
+Runs only where the reference checkout is present; the
 fixtures it writes are committed, so nothing on a GPU host reads the reference.
 
 * kat_scalar.json -- every unitary-score case of the reference's scalar tests
