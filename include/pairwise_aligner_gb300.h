@@ -225,7 +225,7 @@ pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells);
 
 /* Of those, pairs whose sequence2 has at most `max_rows` rows (few 512-row passes) run on
  * teams of 4 warps, two pairs per block, instead of all 8 warps of a block (beside
- * them, on the SMs their blocks release); default 8192 (16 passes), 0 keeps every
+ * them, on the SMs their blocks release); default 12288 (24 passes), 0 keeps every
  * such pair on whole blocks. */
 pa_status pa_set_team_threshold(pa_ctx *ctx, uint32_t max_rows);
 

@@ -69,7 +69,7 @@ struct pa_ctx {
     int64_t long_cells = 1ll << 20;   // pairs with at least this many cells use CTA mode
     int64_t huge_cells = 1ll << 28;   // ... and with this many (and n >= huge_min_n) cluster mode
     int32_t huge_min_n = 8192;
-    int32_t team_max_n = 8192;        // CTA-mode pairs with at most this many rows run on 4-warp teams
+    int32_t team_max_n = 12288;       // CTA-mode pairs with at most this many rows run on 4-warp teams
     int64_t want_ring_m = 0;          // the next call's longest CTA-mode sequence1 (host: exact)
     DevBuf in_seq1, in_off1, in_seq2, in_off2, in_out;   // staging for the host-buffer entry points
     int G[3] = {kDefaultG, kDefaultG, kDefaultG};
