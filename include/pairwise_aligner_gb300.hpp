@@ -342,6 +342,67 @@ private:
     std::shared_ptr<pa_ctx> _ctx;
 };
 
+// ---- input path -------------------------------------------------------------------------------
+
+// A FASTA / FASTQ file in the batch layout (pa_seqfile_*): record k is
+// sequences.substr(offsets[k], offsets[k + 1] - offsets[k]); qualities likewise (FASTQ only).
+struct sequence_file {
+    std::vector<std::string> names;
+    std::string sequences;
+    std::vector<uint64_t> offsets{0};
+    std::string qualities;
+
+    size_t size() const noexcept { return names.size(); }
+    std::string_view sequence(size_t k) const
+    {
+        return std::string_view{sequences}.substr(offsets[k], offsets[k + 1] - offsets[k]);
+    }
+};
+
+namespace detail {
+inline sequence_file take_seqfile(pa_seqfile *f)
+{
+    sequence_file out;
+    const uint64_t n = pa_seqfile_count(f);
+    const uint64_t *off = pa_seqfile_offsets(f);
+    out.offsets.assign(off, off + n + 1);
+    const uint8_t *seq = pa_seqfile_sequences(f);
+    out.sequences.assign(reinterpret_cast<const char *>(seq), off[n]);
+    if (const uint8_t *q = pa_seqfile_qualities(f)) out.qualities.assign(reinterpret_cast<const char *>(q), off[n]);
+    out.names.reserve(n);
+    for (uint64_t k = 0; k < n; ++k) out.names.emplace_back(pa_seqfile_name(f, k));
+    pa_seqfile_free(f);
+    return out;
+}
+}  // namespace detail
+
+// Read a FASTA or FASTQ file; a malformed record throws with its line number.
+inline sequence_file read_sequences(std::string const &path)
+{
+    pa_seqfile *f = nullptr;
+    char err[256] = {};
+    if (pa_seqfile_read(path.c_str(), &f, err, sizeof(err)) != PA_OK) throw std::runtime_error(err);
+    return detail::take_seqfile(f);
+}
+
+inline sequence_file parse_sequences(std::string_view text)
+{
+    pa_seqfile *f = nullptr;
+    char err[256] = {};
+    if (pa_seqfile_parse(text.data(), text.size(), &f, err, sizeof(err)) != PA_OK) throw std::runtime_error(err);
+    return detail::take_seqfile(f);
+}
+
+// 2-bit DNA words (16 bases per word, A/a 0, C/c 1, G/g 2, T/t 3); `invalid` counts other bytes.
+inline std::vector<uint32_t> pack_2bit(std::string_view bases, uint64_t *invalid = nullptr)
+{
+    std::vector<uint32_t> words((bases.size() + 15) / 16);
+    uint64_t bad = 0;
+    pa_pack_2bit_host(reinterpret_cast<const uint8_t *>(bases.data()), bases.size(), words.data(), &bad);
+    if (invalid) *invalid = bad;
+    return words;
+}
+
 namespace cfg {
 // cfg::configure_aligner(rule) -> aligner (configure_aligner.hpp:165-206).
 template <configuration_rule rule_t>

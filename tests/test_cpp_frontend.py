@@ -83,3 +83,28 @@ def test_cpp_frontend_reference_kats(runner, kats):
                          check=True).stdout.split("\n")
     for c, line in zip(kats, out):
         assert int(line.split()[0]) == c["expected_score"], (c["source"], c["name"], line)
+
+
+def test_cpp_sequence_file_reader(built_lib, tmp_path, oracle):
+    """read_sequences / pack_2bit of the C++ front end (host code: runs without a GPU)."""
+    import numpy as np
+    from pairwise_aligner_gb300 import seqio
+    exe = str(tmp_path / "seqfile_dump")
+    libdir = os.path.dirname(built_lib)
+    subprocess.check_call(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-Werror",
+                           "-I", os.path.join(REPO, "include"), os.path.join(REPO, "tests", "cpp", "seqfile_dump.cpp"),
+                           "-L", libdir, "-lpa_gb300", f"-Wl,-rpath,{libdir}", "-o", exe])
+    text = b"@r1 first\nACGTNACGT\n+\nIIIIIIIII\n@r2\n\n+\n\n@r3\r\nacgtacgtacgtacgtAC\r\n+r3\r\nJJJJJJJJJJJJJJJJJJ\r\n"
+    path = tmp_path / "reads.fastq"
+    path.write_bytes(text)
+    out = subprocess.run([exe, str(path)], capture_output=True, text=True, check=True).stdout.split("\n")
+    f = seqio.read_sequences(str(path))
+    for k in range(len(f)):
+        name, seq, qual = out[k].split("\t")
+        q = f.qual[int(f.off[k]):int(f.off[k + 1])].tobytes().decode()
+        assert (name, seq, qual) == (f.names[k], f.sequence(k).decode() or "-", q or "-")
+    words, bad = oracle.pack_2bit(f.seq)
+    assert out[len(f)].split() == [str(int(w)) for w in words] and int(out[len(f) + 1]) == bad
+    path.write_bytes(b"@r\nACG\n+\nII\n")
+    r = subprocess.run([exe, str(path)], capture_output=True, text=True)
+    assert r.returncode == 1 and "line 4" in r.stdout
