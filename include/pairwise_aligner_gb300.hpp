@@ -309,6 +309,23 @@ public:
         return res;
     }
 
+    // Bulk over 2-bit packed DNA (pa_align_batch_packed; see pack_2bit): pair k is bases
+    // [off1[k], off1[k+1]) of words1 against [off2[k], off2[k+1]) of words2.
+    std::vector<pa_result> compute_packed(std::vector<uint32_t> const &words1, std::vector<uint64_t> const &off1,
+                                          std::vector<uint32_t> const &words2, std::vector<uint64_t> const &off2)
+    {
+        if (off1.size() != off2.size() || off1.empty())
+            throw std::runtime_error("both collections must hold the same number of sequences");
+        if (words1.size() * 16 < off1.back() || words2.size() * 16 < off2.back())
+            throw std::runtime_error("the packed words end before the last offset");
+        const uint64_t n = off1.size() - 1;
+        std::vector<pa_result> out(n);
+        check(pa_align_batch_packed(_ctx.get(), &_cfg, words1.data(), off1.data(), words2.data(), off2.data(), n,
+                                    out.data(), nullptr),
+              _ctx.get());
+        return out;
+    }
+
     // Single pair (interface_one_to_one_single.hpp:44-67).
     aligner_result compute(std::string_view seq1, std::string_view seq2)
     {
