@@ -173,7 +173,7 @@ def reference_arm(args):
     from pairwise_aligner_gb300 import workloads as W
     d, _ = load_workload(args.pairs, args.workload)
     threads = os.cpu_count() or 1
-    kind, label = "port", "oracle inter-sequence int16 SIMD port (oracle/pa_oracle.c), pthreads"
+    kind, label = "port", "oracle inter-sequence SIMD port, int16x8 / int32x4 lanes (oracle/pa_oracle.c), pthreads"
     ref_lib = os.path.join(REPO, "oracle", "_ref", "libpa_ref.so")
     if os.path.exists(ref_lib):
         kind, label = "reference", "reference headers built by oracle/ref_build.py"
@@ -194,7 +194,7 @@ def reference_arm(args):
     sample = f"first {n} of {len(d['off1']) - 1} pairs ({cells:.3g} cells) per step; {label}"
     line = {"impl": "reference", "metric": METRIC if d["local"] else METRIC_GLOBAL, "value": round(value, 3), "unit": "GCUPS", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16 lanes",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16 lanes (int32 where needed)",
             "data": "synthetic", "config": {"workload": workload_name(d, args.workload, len(d["off1"]) - 1),
                                             "pairs_per_step": n},
             "cpu_baseline": {"value": round(value, 3), "unit": "GCUPS", "cores": threads, "kind": kind,
@@ -391,7 +391,7 @@ def our_arm(args):
         threads = os.cpu_count() or 1
         rate, npairs, dt = cpu_sample_rate(d, args.cpu_seconds, threads)
         line["cpu_baseline"] = {"value": round(rate, 3), "unit": "GCUPS", "cores": threads, "kind": "port",
-                                "sample": f"first {npairs} pairs of the batch, {dt:.1f} s, oracle int16 SIMD port"}
+                                "sample": f"first {npairs} pairs of the batch, {dt:.1f} s, oracle SIMD port (int16x8 / int32x4)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -27,8 +27,9 @@
  *  2. pa_oracle_simd_batch -- a multi-threaded inter-sequence SIMD port of the
  *     reference's fixed-width SIMD path (cfg::score_model_unitary_simd,
  *     include/pairwise_aligner/configuration/score_model_unitary_simd.hpp:51-137):
- *     one alignment per int16 vector lane, GCC vector extensions (portable to
- *     x86 SSE and Arm NEON), pthreads over batches.  Scores only, like the
+ *     one alignment per vector lane (8 int16 lanes, or 4 int32 lanes for pairs
+ *     whose scores could overflow int16), 16-byte GCC vector extensions (native
+ *     on x86 SSE2 and Arm NEON), pthreads over batches.  Scores only, like the
  *     reference.  It is the timed CPU baseline where the reference itself can
  *     not be built.
  *
@@ -357,11 +358,14 @@ int pa_oracle_align_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint6
 /* inter-sequence SIMD port (CPU baseline), scores only                        */
 /* ------------------------------------------------------------------------- */
 
-#define PA_LANES 16
-typedef int16_t v16s __attribute__((vector_size(32)));
-
-static inline v16s vsel(v16s mask, v16s a, v16s b) { return (a & mask) | (b & ~mask); }
-static inline v16s vmax(v16s a, v16s b) { return vsel((v16s)(a > b), a, b); }
+/* Two lane types, as the reference's fixed-width SIMD model offers them
+ * (score_model_unitary_simd<int16_t|int32_t>, score_model_unitary_simd.hpp:51-137):
+ * int16 lanes for pairs whose scores fit int16, int32 lanes for the rest.  The vectors are
+ * 16 bytes, the width both baseline ISAs have natively (SSE2 on x86-64, NEON on AArch64):
+ * GCC lowers wider generic vectors to scalar code where the target lacks them, which made an
+ * earlier 32-byte build 17x slower per thread than its AVX2 build. */
+typedef int16_t v8s __attribute__((vector_size(16)));
+typedef int32_t v4i __attribute__((vector_size(16)));
 
 typedef struct {
     const pa_oracle_cfg *cfg;
@@ -375,112 +379,123 @@ typedef struct {
     int rc;
 } simd_ctx;
 
-/* One batch of up to PA_LANES pairs, one pair per int16 lane.  Like the
- * reference's bulk vectors (dp_vector_bulk.hpp:83-103) the lanes are padded to
- * the longest pair; padding symbols never match and padded cells never feed a
- * real cell, so only the per-lane result cell needs care. */
-static int simd_batch(simd_ctx *x, const uint32_t *ids, int lanes, uint8_t *qbuf, uint8_t *tbuf,
-                      v16s *hrow, v16s *vgap, size_t cap_n)
-{
-    const pa_oracle_cfg *c = x->cfg;
-    const int local = c->local != 0;
-    uint64_t mmax = 0, nmax = 0, ml[PA_LANES], nl[PA_LANES];
-    for (int l = 0; l < PA_LANES; ++l) {
-        uint32_t k = ids[l < lanes ? l : 0];
-        ml[l] = x->off1[k + 1] - x->off1[k];
-        nl[l] = x->off2[k + 1] - x->off2[k];
-        if (ml[l] > mmax) mmax = ml[l];
-        if (nl[l] > nmax) nmax = nl[l];
-    }
-    if (nmax + 1 > cap_n) return PA_ORACLE_ENOMEM;
-    /* transpose: qbuf[i*L + l], tbuf[j*L + l]; pads 0x00 (query) / 0x01 (target) */
-    for (int l = 0; l < PA_LANES; ++l) {
-        uint32_t k = ids[l < lanes ? l : 0];
-        const uint8_t *a = x->s1 + x->off1[k], *b = x->s2 + x->off2[k];
-        for (uint64_t i = 0; i < mmax; ++i) qbuf[i * PA_LANES + l] = i < ml[l] ? a[i] : 0x00;
-        for (uint64_t j = 0; j < nmax; ++j) tbuf[j * PA_LANES + l] = j < nl[l] ? b[j] : 0x01;
-    }
-    const int16_t goe = (int16_t)(c->gap_open + c->gap_extension), ext = (int16_t)c->gap_extension;
-    const int fcf = local || c->first_column_free, frf = local || c->first_row_free;
-    v16s vgoe, vext, vmatch, vmis, zero, best;
-    for (int l = 0; l < PA_LANES; ++l) {
-        vgoe[l] = goe; vext[l] = ext; vmatch[l] = (int16_t)c->match; vmis[l] = (int16_t)c->mismatch;
-        zero[l] = 0; best[l] = INT16_MIN;
-    }
-    for (uint64_t j = 0; j <= nmax; ++j) {
-        int16_t h = (!frf && j > 0) ? (int16_t)(c->gap_open + c->gap_extension * (int64_t)j) : 0;
-        for (int l = 0; l < PA_LANES; ++l) { hrow[j][l] = h; vgap[j][l] = (int16_t)(h + goe); }
-    }
-    int32_t res[PA_LANES];
-    for (int l = 0; l < PA_LANES; ++l) if (!local && ml[l] == 0) res[l] = hrow[nl[l]][l];
-    for (uint64_t i = 1; i <= mmax; ++i) {
-        int16_t hc = (!fcf) ? (int16_t)(c->gap_open + c->gap_extension * (int64_t)i) : 0;
-        v16s hgap, diag = hrow[0];
-        for (int l = 0; l < PA_LANES; ++l) { hgap[l] = (int16_t)(hc + goe); hrow[0][l] = hc; }
-        v16s qa;
-        for (int l = 0; l < PA_LANES; ++l) qa[l] = qbuf[(i - 1) * PA_LANES + l];
-        for (uint64_t j = 1; j <= nmax; ++j) {
-            v16s tb;
-            for (int l = 0; l < PA_LANES; ++l) tb[l] = tbuf[(j - 1) * PA_LANES + l];
-            v16s d = diag + vsel((v16s)(qa == tb), vmatch, vmis);
-            if (local) d = vmax(d, zero);
-            v16s h = vmax(vmax(d, vgap[j]), hgap);
-            diag = hrow[j];
-            hrow[j] = h;
-            if (local) best = vmax(best, h);
-            v16s hoe = h + vgoe;
-            vgap[j] = vmax(vgap[j] + vext, hoe);
-            hgap = vmax(hgap + vext, hoe);
-        }
-        if (!local)
-            for (int l = 0; l < PA_LANES; ++l) if (ml[l] == i) res[l] = hrow[nl[l]][l];
-    }
-    for (int l = 0; l < lanes; ++l) {
-        if (local) res[l] = (ml[l] == 0 || nl[l] == 0) ? INT32_MIN : best[l];
-        x->scores[ids[l]] = res[l];
-    }
-    return PA_ORACLE_OK;
+/* One batch of up to L pairs, one pair per lane (VT: L lanes of ST).  Like the reference's
+ * bulk vectors (dp_vector_bulk.hpp:83-103) the lanes are padded to the longest pair; padding
+ * symbols (0x200 in sequence1, 0x300 in sequence2) never match a byte, and padded cells
+ * never feed a real cell, so only the per-lane result cell needs care.  Both sequences are
+ * widened to lane vectors once per batch, so the inner loop is vector operations only. */
+/* lane-wise max of two vectors (C has no vector ?:; the comparison is an all-ones lane mask) */
+#define PA_VMAX(VT, A, B) ({ VT a_ = (A), b_ = (B); VT m_ = (VT)(a_ > b_); (a_ & m_) | (b_ & ~m_); })
+
+#define PA_SIMD_BATCH(FN, VT, ST, L, ST_MIN)                                                        \
+static int FN(simd_ctx *x, const uint32_t *ids, int lanes, VT *qvec, VT *tvec, VT *hrow, VT *vgap,  \
+              size_t cap_n)                                                                        \
+{                                                                                                  \
+    const pa_oracle_cfg *c = x->cfg;                                                              \
+    const int local = c->local != 0;                                                              \
+    uint64_t mmax = 0, nmax = 0, ml[L], nl[L];                                                    \
+    for (int l = 0; l < L; ++l) {                                                                 \
+        uint32_t k = ids[l < lanes ? l : 0];                                                      \
+        ml[l] = x->off1[k + 1] - x->off1[k];                                                      \
+        nl[l] = x->off2[k + 1] - x->off2[k];                                                      \
+        if (ml[l] > mmax) mmax = ml[l];                                                           \
+        if (nl[l] > nmax) nmax = nl[l];                                                           \
+    }                                                                                              \
+    if (nmax + 1 > cap_n || mmax + 1 > cap_n) return PA_ORACLE_ENOMEM;                            \
+    for (int l = 0; l < L; ++l) {                                                                 \
+        uint32_t k = ids[l < lanes ? l : 0];                                                      \
+        const uint8_t *a = x->s1 + x->off1[k], *b = x->s2 + x->off2[k];                          \
+        for (uint64_t i = 0; i < mmax; ++i) qvec[i][l] = (ST)(i < ml[l] ? a[i] : 0x200);         \
+        for (uint64_t j = 0; j < nmax; ++j) tvec[j][l] = (ST)(j < nl[l] ? b[j] : 0x300);         \
+    }                                                                                              \
+    const ST goe = (ST)(c->gap_open + c->gap_extension), ext = (ST)c->gap_extension;             \
+    const int fcf = local || c->first_column_free, frf = local || c->first_row_free;             \
+    VT vgoe, vext, vmatch, vmis, zero, best;                                                      \
+    for (int l = 0; l < L; ++l) {                                                                 \
+        vgoe[l] = goe; vext[l] = ext; vmatch[l] = (ST)c->match; vmis[l] = (ST)c->mismatch;       \
+        zero[l] = 0; best[l] = ST_MIN;                                                            \
+    }                                                                                              \
+    for (uint64_t j = 0; j <= nmax; ++j) {                                                        \
+        ST h = (!frf && j > 0) ? (ST)(c->gap_open + c->gap_extension * (int64_t)j) : 0;          \
+        for (int l = 0; l < L; ++l) { hrow[j][l] = h; vgap[j][l] = (ST)(h + goe); }              \
+    }                                                                                              \
+    int32_t res[L];                                                                                \
+    for (int l = 0; l < L; ++l) if (!local && ml[l] == 0) res[l] = hrow[nl[l]][l];               \
+    for (uint64_t i = 1; i <= mmax; ++i) {                                                        \
+        ST hc = (!fcf) ? (ST)(c->gap_open + c->gap_extension * (int64_t)i) : 0;                  \
+        VT hgap, diag = hrow[0];                                                                  \
+        for (int l = 0; l < L; ++l) { hgap[l] = (ST)(hc + goe); hrow[0][l] = hc; }               \
+        const VT qa = qvec[i - 1];                                                                \
+        for (uint64_t j = 1; j <= nmax; ++j) {                                                    \
+            VT eq = (VT)(qa == tvec[j - 1]);                                                      \
+            VT d = diag + ((vmatch & eq) | (vmis & ~eq));                                         \
+            if (local) d = PA_VMAX(VT, d, zero);                                                  \
+            VT g = vgap[j];                                                                        \
+            VT h = PA_VMAX(VT, PA_VMAX(VT, d, g), hgap);                                          \
+            diag = hrow[j];                                                                        \
+            hrow[j] = h;                                                                           \
+            if (local) best = PA_VMAX(VT, best, h);                                              \
+            VT hoe = h + vgoe;                                                                    \
+            VT ge = g + vext, he = hgap + vext;                                                   \
+            vgap[j] = PA_VMAX(VT, ge, hoe);                                                       \
+            hgap = PA_VMAX(VT, he, hoe);                                                          \
+        }                                                                                          \
+        if (!local)                                                                                \
+            for (int l = 0; l < L; ++l) if (ml[l] == i) res[l] = hrow[nl[l]][l];                  \
+    }                                                                                              \
+    for (int l = 0; l < lanes; ++l) {                                                             \
+        if (local) res[l] = (ml[l] == 0 || nl[l] == 0) ? INT32_MIN : best[l];                    \
+        x->scores[ids[l]] = res[l];                                                               \
+    }                                                                                              \
+    return PA_ORACLE_OK;                                                                          \
 }
 
-static void *simd_worker(void *p)
-{
-    simd_ctx *x = (simd_ctx *)p;
-    size_t cap_n = 0;
-    uint8_t *qbuf = NULL, *tbuf = NULL;
-    v16s *hrow = NULL, *vgap = NULL;
-    for (;;) {
-        pthread_mutex_lock(&x->lock);
-        uint64_t b = x->next_batch++;
-        int rc_seen = x->rc;
-        pthread_mutex_unlock(&x->lock);
-        uint64_t first = b * PA_LANES;
-        if (rc_seen || first >= x->n_pairs) break;
-        int lanes = (int)((x->n_pairs - first) < PA_LANES ? (x->n_pairs - first) : PA_LANES);
-        const uint32_t *ids = x->order + first;
-        uint64_t mmax = 0, nmax = 0;
-        for (int l = 0; l < lanes; ++l) {
-            uint64_t m = x->off1[ids[l] + 1] - x->off1[ids[l]], n = x->off2[ids[l] + 1] - x->off2[ids[l]];
-            if (m > mmax) mmax = m;
-            if (n > nmax) nmax = n;
-        }
-        if (nmax + 1 > cap_n || mmax + 1 > cap_n) {
-            cap_n = (nmax > mmax ? nmax : mmax) + 1;
-            free(qbuf); free(tbuf); free(hrow); free(vgap);
-            qbuf = (uint8_t *)malloc(cap_n * PA_LANES);
-            tbuf = (uint8_t *)malloc(cap_n * PA_LANES);
-            hrow = (v16s *)aligned_alloc(32, cap_n * sizeof(v16s));
-            vgap = (v16s *)aligned_alloc(32, cap_n * sizeof(v16s));
-            if (!qbuf || !tbuf || !hrow || !vgap) {
-                pthread_mutex_lock(&x->lock); x->rc = PA_ORACLE_ENOMEM; pthread_mutex_unlock(&x->lock);
-                break;
-            }
-        }
-        int rc = simd_batch(x, ids, lanes, qbuf, tbuf, hrow, vgap, cap_n);
-        if (rc) { pthread_mutex_lock(&x->lock); x->rc = rc; pthread_mutex_unlock(&x->lock); break; }
-    }
-    free(qbuf); free(tbuf); free(hrow); free(vgap);
-    return NULL;
+PA_SIMD_BATCH(simd_batch16, v8s, int16_t, 8, INT16_MIN)
+PA_SIMD_BATCH(simd_batch32, v4i, int32_t, 4, INT32_MIN)
+
+/* Workers pull batches of the lane count from a shared counter; each keeps its buffers. */
+#define PA_SIMD_WORKER(FN, BATCH, VT, L)                                                           \
+static void *FN(void *p)                                                                           \
+{                                                                                                  \
+    simd_ctx *x = (simd_ctx *)p;                                                                  \
+    size_t cap_n = 0;                                                                              \
+    VT *qvec = NULL, *tvec = NULL, *hrow = NULL, *vgap = NULL;                                    \
+    for (;;) {                                                                                     \
+        pthread_mutex_lock(&x->lock);                                                             \
+        uint64_t b = x->next_batch++;                                                             \
+        int rc_seen = x->rc;                                                                       \
+        pthread_mutex_unlock(&x->lock);                                                           \
+        uint64_t first = b * L;                                                                    \
+        if (rc_seen || first >= x->n_pairs) break;                                                \
+        int lanes = (int)((x->n_pairs - first) < L ? (x->n_pairs - first) : L);                  \
+        const uint32_t *ids = x->order + first;                                                   \
+        uint64_t mmax = 0, nmax = 0;                                                              \
+        for (int l = 0; l < lanes; ++l) {                                                         \
+            uint64_t m = x->off1[ids[l] + 1] - x->off1[ids[l]], n = x->off2[ids[l] + 1] - x->off2[ids[l]]; \
+            if (m > mmax) mmax = m;                                                               \
+            if (n > nmax) nmax = n;                                                               \
+        }                                                                                          \
+        if (nmax + 1 > cap_n || mmax + 1 > cap_n) {                                               \
+            cap_n = (nmax > mmax ? nmax : mmax) + 1;                                              \
+            free(qvec); free(tvec); free(hrow); free(vgap);                                       \
+            qvec = (VT *)aligned_alloc(16, cap_n * sizeof(VT));                                   \
+            tvec = (VT *)aligned_alloc(16, cap_n * sizeof(VT));                                   \
+            hrow = (VT *)aligned_alloc(16, cap_n * sizeof(VT));                                   \
+            vgap = (VT *)aligned_alloc(16, cap_n * sizeof(VT));                                   \
+            if (!qvec || !tvec || !hrow || !vgap) {                                               \
+                pthread_mutex_lock(&x->lock); x->rc = PA_ORACLE_ENOMEM; pthread_mutex_unlock(&x->lock); \
+                break;                                                                             \
+            }                                                                                      \
+        }                                                                                          \
+        int rc = BATCH(x, ids, lanes, qvec, tvec, hrow, vgap, cap_n);                            \
+        if (rc) { pthread_mutex_lock(&x->lock); x->rc = rc; pthread_mutex_unlock(&x->lock); break; } \
+    }                                                                                              \
+    free(qvec); free(tvec); free(hrow); free(vgap);                                               \
+    return NULL;                                                                                   \
 }
+
+PA_SIMD_WORKER(simd_worker16, simd_batch16, v8s, 8)
+PA_SIMD_WORKER(simd_worker32, simd_batch32, v4i, 4)
 
 static const uint64_t *g_sort_off1, *g_sort_off2;
 static int cmp_shape(const void *pa, const void *pb)
@@ -493,15 +508,27 @@ static int cmp_shape(const void *pa, const void *pb)
     return a < b ? -1 : (a > b);
 }
 
-/* Worst |value| an int16 lane can see for this pair; mirrors the overflow
- * guard a caller of the reference's int16 SIMD model must respect. */
-static int fits_int16(const pa_oracle_cfg *c, uint64_t m, uint64_t n)
+/* Worst |value| a lane can see for this pair; mirrors the overflow guard a caller of the
+ * reference's int16 / int32 SIMD models must respect. */
+static int64_t lane_bound(const pa_oracle_cfg *c, uint64_t m, uint64_t n)
 {
     int64_t a = llabs((int64_t)c->match), b = llabs((int64_t)c->mismatch);
     int64_t o = llabs((int64_t)c->gap_open), e = llabs((int64_t)c->gap_extension);
     int64_t s = a > b ? a : b;
-    int64_t bound = s * (int64_t)(m < n ? m : n) + 2 * o + e * (int64_t)(m + n + 2) + o + e;
-    return bound < 32000;
+    return s * (int64_t)(m < n ? m : n) + 2 * o + e * (int64_t)(m + n + 2) + o + e;
+}
+
+static int run_simd(simd_ctx *x, void *(*worker)(void *), int nthreads)
+{
+    pthread_mutex_init(&x->lock, NULL);
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!th) { pthread_mutex_destroy(&x->lock); return PA_ORACLE_ENOMEM; }
+    for (int t = 1; t < nthreads; ++t) pthread_create(&th[t], NULL, worker, x);
+    worker(x);
+    for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+    free(th);
+    pthread_mutex_destroy(&x->lock);
+    return x->rc;
 }
 
 int pa_oracle_simd_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint64_t *off1,
@@ -511,13 +538,16 @@ int pa_oracle_simd_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint64
     if (!c || !scores || (n_pairs && (!off1 || !off2))) return PA_ORACLE_EINVAL;
     if (c->local == 0 && (c->last_column_free || c->last_row_free)) return PA_ORACLE_EINVAL;
     if (c->dim) return PA_ORACLE_EINVAL;                /* the SIMD port scores unitary only */
-    uint32_t *order = (uint32_t *)malloc(sizeof(uint32_t) * (n_pairs ? n_pairs : 1));
+    uint32_t *order = (uint32_t *)malloc(sizeof(uint32_t) * (n_pairs ? n_pairs : 1) * 2);
     if (!order) return PA_ORACLE_ENOMEM;
-    uint64_t n_simd = 0;
+    uint32_t *order32 = order + (n_pairs ? n_pairs : 1);
+    uint64_t n16 = 0, n32 = 0;
     for (uint64_t k = 0; k < n_pairs; ++k) {
         uint64_t m = off1[k + 1] - off1[k], n = off2[k + 1] - off2[k];
-        if (fits_int16(c, m, n)) order[n_simd++] = (uint32_t)k;
-        else {                                    /* too wide for int16 lanes: scalar int64 */
+        const int64_t bound = lane_bound(c, m, n);
+        if (bound < 32000) order[n16++] = (uint32_t)k;
+        else if (bound < (1ll << 30)) order32[n32++] = (uint32_t)k;
+        else {                                    /* too wide for int32 lanes: scalar int64 */
             int64_t sc, e1, e2;
             int rc = pa_oracle_align(c, s1 + off1[k], m, s2 + off2[k], n, &sc, &e1, &e2);
             if (rc) { free(order); return rc; }
@@ -525,19 +555,18 @@ int pa_oracle_simd_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint64
         }
     }
     g_sort_off1 = off1; g_sort_off2 = off2;
-    qsort(order, n_simd, sizeof(uint32_t), cmp_shape);
+    qsort(order, n16, sizeof(uint32_t), cmp_shape);
+    qsort(order32, n32, sizeof(uint32_t), cmp_shape);
+    if (nthreads < 1) nthreads = 1;
     simd_ctx x;
     memset(&x, 0, sizeof(x));
-    x.cfg = c; x.s1 = s1; x.off1 = off1; x.s2 = s2; x.off2 = off2;
-    x.order = order; x.n_pairs = n_simd; x.scores = scores;
-    pthread_mutex_init(&x.lock, NULL);
-    if (nthreads < 1) nthreads = 1;
-    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
-    for (int t = 1; t < nthreads; ++t) pthread_create(&th[t], NULL, simd_worker, &x);
-    simd_worker(&x);
-    for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
-    free(th);
-    pthread_mutex_destroy(&x.lock);
+    x.cfg = c; x.s1 = s1; x.off1 = off1; x.s2 = s2; x.off2 = off2; x.scores = scores;
+    x.order = order; x.n_pairs = n16;
+    int rc = n16 ? run_simd(&x, simd_worker16, nthreads) : PA_ORACLE_OK;
+    if (!rc && n32) {
+        x.order = order32; x.n_pairs = n32; x.next_batch = 0; x.rc = 0;
+        rc = run_simd(&x, simd_worker32, nthreads);
+    }
     free(order);
-    return x.rc;
+    return rc;
 }
