@@ -126,3 +126,33 @@ def test_oracle_symmetry(oracle, local):
         a = rng.choice(list(b"ACGT"), size=int(rng.integers(1, 40))).astype(np.uint8).tobytes()
         b = rng.choice(list(b"ACGT"), size=int(rng.integers(1, 40))).astype(np.uint8).tobytes()
         assert oracle.align(cfg, a, b)[0] == oracle.align(cfg, b, a)[0]
+
+
+def test_simd_port_matches_scalar_on_random_configs(oracle):
+    """The timed CPU port (int16x8 lanes, int32x4 lanes where int16 could overflow) equals the
+    scalar restatement across score models, methods and lengths."""
+    from pairwise_aligner_gb300.aligner import pack
+    rng = np.random.default_rng(31)
+    acgt = np.frombuffer(b"ACGT", dtype=np.uint8)
+    for trial in range(24):
+        match, mismatch = int(rng.integers(1, 6)), int(-rng.integers(1, 7))
+        go, ge = int(-rng.integers(0, 11)), int(-rng.integers(1, 4))
+        local = bool(trial % 2)
+        fc, fr = (False, False) if local else (bool(rng.integers(0, 2)), bool(rng.integers(0, 2)))
+        cfg = oracle.make_cfg(match, mismatch, go, ge, local=local, first_column_free=fc, first_row_free=fr)
+        long_pairs = trial % 3 == 0                       # lengths that push some pairs to int32 lanes
+        lens = rng.integers(0, 3000 if long_pairs else 300, size=(40, 2))
+        s1, s2 = [], []
+        for m, n in lens:
+            a = acgt[rng.integers(0, 4, int(m))]
+            b = a[: int(n)].copy() if rng.random() < 0.5 else acgt[rng.integers(0, 4, int(n))]
+            b = np.concatenate([b, acgt[rng.integers(0, 4, max(0, int(n) - len(b)))]])
+            flip = rng.random(len(b)) < 0.1
+            b[flip] = acgt[rng.integers(0, 4, int(flip.sum()))]
+            s1.append(a.tobytes())
+            s2.append(b.tobytes())
+        q, qo = pack(s1)
+        t, to = pack(s2)
+        got = oracle.simd_batch(cfg, q, qo, t, to, nthreads=4)
+        want, _, _ = oracle.align_batch(cfg, q, qo, t, to, nthreads=4)
+        assert list(got) == list(want), (trial, match, mismatch, go, ge, local, fc, fr)
