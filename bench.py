@@ -174,9 +174,6 @@ def reference_arm(args):
     d, _ = load_workload(args.pairs, args.workload)
     threads = os.cpu_count() or 1
     kind, label = "port", "oracle inter-sequence SIMD port, int16x8 / int32x4 lanes (oracle/pa_oracle.c), pthreads"
-    ref_lib = os.path.join(REPO, "oracle", "_ref", "libpa_ref.so")
-    if os.path.exists(ref_lib):
-        kind, label = "reference", "reference headers built by oracle/ref_build.py"
     # one step = a bounded leading sample, sized so W + K steps take about two minutes
     per_step = max(0.5, min(5.0, 100.0 / max(1, args.steps + args.warmup)))
     rate, n, dt = cpu_sample_rate(d, per_step, threads)
