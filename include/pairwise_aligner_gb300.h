@@ -96,8 +96,13 @@ typedef struct pa_result {
 #define PA_RESULT_BANDED     0x02u  /* certified banded result                              */
 #define PA_RESULT_FULL_DP    0x04u  /* band fell back to the full DP                        */
 #define PA_RESULT_TRIVIAL    0x08u  /* an empty sequence: answered without a DP             */
-#define PA_RESULT_OVERFLOW   0x10u  /* pa_align_batch_device_static only: the pair's scores
-                                       could exceed int32; score is INT32_MIN                */
+#define PA_RESULT_OVERFLOW   0x10u  /* the pair's scores could exceed int32: not aligned,
+                                       score INT32_MIN (the call returns PA_ERR_OVERFLOW when
+                                       it reports errors)                                     */
+#define PA_RESULT_ERROR      0x20u  /* no valid score, INT32_MIN: the pair's offsets are
+                                       inconsistent (a device entry point, see below), a
+                                       symbol is outside the substitution matrix, or a
+                                       bounded device wait gave up (PA_ERR_TIMEOUT)           */
 
 /* Context options; zero-initialised means defaults. */
 typedef struct pa_options {
@@ -147,7 +152,14 @@ pa_status pa_align_batch(pa_ctx *ctx, const pa_config *config,
  * Asynchronous on `stream` (a cudaStream_t; NULL = the context's stream,
  * cudaStreamLegacy / cudaStreamPerThread are accepted);
  * seq1_bytes / seq2_bytes are the sizes of the two byte buffers.  When stats
- * is non-NULL the call synchronises to fill it. */
+ * is non-NULL the call synchronises to fill it.
+ * The offsets are checked on the device: if any pair has off[k] > off[k+1] or an
+ * offset past seq1_bytes / seq2_bytes, no pair is aligned and every result is
+ * INT32_MIN with PA_RESULT_ERROR.  Errors found on the device (those offsets,
+ * PA_ERR_OVERFLOW, PA_ERR_TIMEOUT, symbols outside a substitution matrix) are
+ * returned as a status only when stats is non-NULL (the call then waits for the
+ * device); without stats the call returns as soon as the work is queued, and the
+ * affected pairs carry PA_RESULT_OVERFLOW / PA_RESULT_ERROR in their results. */
 pa_status pa_align_batch_device(pa_ctx *ctx, const pa_config *config,
                                 const uint8_t *d_seq1, const uint64_t *d_off1, uint64_t seq1_bytes,
                                 const uint8_t *d_seq2, const uint64_t *d_off2, uint64_t seq2_bytes,
@@ -164,14 +176,25 @@ pa_status pa_align_batch_device(pa_ctx *ctx, const pa_config *config,
  *    4,194,304 cells (32 MiB) that every GPU loading the library holds until
  *    the process exits.  seq1_bytes + n_pairs must not exceed 4,194,304,
  *    else PA_ERR_TOO_LARGE is returned and nothing is launched.
- *  - The first call on a device looks up that array's device address
- *    (cudaGetSymbolAddress) with the device current; make that first call
- *    before any stream capture.
+ *  - Every call made outside a stream capture looks up that array's device
+ *    address (cudaGetSymbolAddress) with the device current, so a device that
+ *    was reset is followed.  A call made while `stream` is captured uses the
+ *    address of the last call on that device: make the first call on a device
+ *    before any stream capture (else PA_ERR_UNSUPPORTED).
  *  - All calls share the array: calls whose work overlaps on the GPU (other
  *    streams, other host threads) race.  Serialise them.
- *  - Arithmetic is s32 with raw byte comparison, pairs in input order; a pair
- *    whose scores could exceed int32 gets INT32_MIN and PA_RESULT_OVERFLOW.
- * Results equal those of pa_align_batch_device except the width field (32). */
+ *  - Arithmetic is s32 with raw byte comparison, pairs in input order.
+ *  - Errors are per pair (the call returns before the device runs): a pair
+ *    whose scores could exceed int32 gets INT32_MIN and PA_RESULT_OVERFLOW; a
+ *    pair whose offsets decrease or run past seq1_bytes / seq2_bytes is not
+ *    aligned and gets INT32_MIN and PA_RESULT_ERROR (its scratch row could
+ *    leave the array); other pairs of a batch with such offsets have undefined
+ *    scores, since their scratch rows may overlap.
+ * Scores and end positions equal those of pa_align_batch_device.  The other
+ * fields differ: width is always 32 and PA_RESULT_RERUN never appears; over-
+ * bound pairs are flagged here while pa_align_batch_device also returns
+ * PA_ERR_OVERFLOW when it reports errors; and NULL `stream` means the legacy
+ * default stream here but the context's stream there. */
 pa_status pa_align_batch_device_static(const pa_config *config,
                                        const uint8_t *d_seq1, const uint64_t *d_off1, uint64_t seq1_bytes,
                                        const uint8_t *d_seq2, const uint64_t *d_off2, uint64_t seq2_bytes,
@@ -222,6 +245,12 @@ pa_status pa_mlp_to_bf16(const float *src, int rows, int cols, int ld_dst, void 
  * (the warps of a block pipeline the pair's row passes) instead of one group of
  * lanes; default 2^20.  1 sends every pair there, UINT64_MAX none. */
 pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells);
+
+/* Polls a CTA-mode progress wait makes after its first look before it gives up
+ * (default 2^24, with a short sleep between polls).  A wait that gives up marks its
+ * pair PA_RESULT_ERROR and the call returns PA_ERR_TIMEOUT; 0 gives up at the first
+ * look (tests use it to exercise that path).  No counterpart in the reference. */
+pa_status pa_set_wait_limit(pa_ctx *ctx, uint32_t polls);
 
 /* Of those, pairs whose sequence2 has at most `max_rows` rows (few 512-row passes) run on
  * teams of 4 warps, two pairs per block, instead of all 8 warps of a block (beside

@@ -22,7 +22,7 @@ STATUS = {
     8: "PA_ERR_TOO_LARGE",
 }
 
-RESULT_RERUN, RESULT_BANDED, RESULT_FULL_DP, RESULT_TRIVIAL, RESULT_OVERFLOW = 0x01, 0x02, 0x04, 0x08, 0x10
+RESULT_RERUN, RESULT_BANDED, RESULT_FULL_DP, RESULT_TRIVIAL, RESULT_OVERFLOW, RESULT_ERROR = 0x01, 0x02, 0x04, 0x08, 0x10, 0x20
 
 
 class PaConfig(ctypes.Structure):
@@ -160,6 +160,7 @@ SIGNATURES = {
     "pa_set_cta_threshold": ([_ctxp, ctypes.c_uint64], ctypes.c_int),
     "pa_set_cluster_threshold": ([_ctxp, ctypes.c_uint64, ctypes.c_uint32], ctypes.c_int),
     "pa_set_team_threshold": ([_ctxp, ctypes.c_uint32], ctypes.c_int),
+    "pa_set_wait_limit": ([_ctxp, ctypes.c_uint32], ctypes.c_int),
     "pa_set_band_options": ([_ctxp, ctypes.POINTER(PaBandOptions)], ctypes.c_int),
     "pa_get_band_options": ([_ctxp, ctypes.POINTER(PaBandOptions)], ctypes.c_int),
     "pa_set_band_model": ([_ctxp] + [ctypes.c_void_p] * 6, ctypes.c_int),

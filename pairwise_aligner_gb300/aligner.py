@@ -73,6 +73,10 @@ class Context:
         """Block-mode pairs whose sequence2 has at most `max_rows` rows run on 4-warp teams (0: none)."""
         _lib.check(self.lib.pa_set_team_threshold(self.ptr, int(max_rows)), self.ptr)
 
+    def set_wait_limit(self, polls: int):
+        """Polls a CTA-mode progress wait makes before it gives up (default 2^24; 0: at the first look)."""
+        _lib.check(self.lib.pa_set_wait_limit(self.ptr, int(polls)), self.ptr)
+
     def set_substitution_matrix(self, symbols: bytes, scores):
         """Load the matrix that PA_SCORE_MATRIX calls score with: scores[r1 * dim + r2] for a
         sequence1 symbol of rank r1 (its index in `symbols`) against a sequence2 symbol of rank r2."""

@@ -33,7 +33,8 @@ namespace {
 constexpr int kR = 16;             // rows per thread per lane
 constexpr int64_t kDefaultRingM = 65536;   // device entry points: CTA mode up to this sequence1 length
 constexpr int kDefaultG = 8;       // threads per group
-constexpr int kVariants = 9;       // inner-loop variants (pa_kern_v*.cu)
+constexpr int kVariants = 11;      // inner-loop variants: 0..8 dp_kernel (pa_kern_v*.cu), 9 / 10 dp_short
+constexpr int kShortVariant = 9;   // dp_short (s16x2 unitary short pairs) at 2 resident blocks per SM; 10: at 3
 
 struct DevBuf {
     void *p = nullptr;
@@ -44,8 +45,17 @@ struct GraphKey {
     const void *ptrs[6];
     uint64_t n_pairs, b1, b2;
     pa_config cfg;
+    int32_t G[3], variant[3];      // the launch shapes the call was captured with
+    uint32_t wait_limit;
     bool operator<(const GraphKey &o) const { return std::memcmp(this, &o, sizeof(GraphKey)) < 0; }
 };
+
+// A captured call and when it was last replayed (calls of the context count up).
+struct GraphEntry {
+    cudaGraphExec_t exec;
+    uint64_t last_use;
+};
+constexpr size_t kMaxGraphs = 8;   // captured calls kept per context; the least recently used goes first
 
 }  // namespace
 
@@ -63,6 +73,7 @@ struct pa_ctx {
     std::string err;
     // device work buffers (grow only)
     DevBuf keys, order, hist, starts, cursor, sums, ranges, counts, qtab, boundary, rerun, counters, pstats;
+    DevBuf slots;                 // short-pair kernel: 16-byte column slots, (seq1_bytes + n_pairs)
     DevBuf ring, rerun_long;      // CTA mode: boundary rows per block; s16 long pairs to redo in s32
     int32_t ring_m = 0;           // longest sequence1 the ring rows hold (0: no CTA mode yet)
     int ring_grid = 0;            // blocks of every CTA-mode launch
@@ -70,6 +81,7 @@ struct pa_ctx {
     int64_t huge_cells = 1ll << 28;   // ... and with this many (and n >= huge_min_n) cluster mode
     int32_t huge_min_n = 8192;
     int32_t team_max_n = 12288;       // CTA-mode pairs with at most this many rows run on 4-warp teams
+    uint32_t wait_limit = kSpinLimit; // polls of a CTA-mode progress wait before it gives up
     int64_t want_ring_m = 0;          // the next call's longest CTA-mode sequence1 (host: exact)
     DevBuf in_seq1, in_off1, in_seq2, in_off2, in_out;   // staging for the host-buffer entry points
     int G[3] = {kDefaultG, kDefaultG, kDefaultG};
@@ -77,7 +89,8 @@ struct pa_ctx {
     pa_tuning tuning{};           // per method (0 local, 1 global); applied to G/variant per call
     bool fixed_G = false, fixed_variant = false;
     int grid[3] = {0, 0, 0};
-    std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::map<GraphKey, GraphEntry> graphs;
+    uint64_t graph_clock = 0;
     uint64_t last_launches = 0;
     // band mode
     pa_band_options band_opt{1.25f, 16, 64, 0.5f, 6, {0, 0, 0}};
@@ -120,6 +133,12 @@ pa_status fail(pa_ctx *c, pa_status s, const std::string &msg)
                                            cudaGetErrorString(e_));                         \
     } while (0)
 
+void drop_graphs(pa_ctx *c)
+{
+    for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
+    c->graphs.clear();
+}
+
 pa_status ensure(pa_ctx *c, DevBuf &b, size_t bytes)
 {
     if (bytes == 0) bytes = 16;
@@ -135,8 +154,7 @@ pa_status ensure(pa_ctx *c, DevBuf &b, size_t bytes)
     }
     b.cap = want;
     // a grown buffer invalidates captured graphs
-    for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
-    c->graphs.clear();
+    drop_graphs(c);
     return PA_OK;
 }
 
@@ -226,6 +244,23 @@ void pack_2bit_launch(const uint8_t *in, uint64_t n, uint32_t *words, unsigned l
 void unpack_2bit_launch(const uint32_t *words, uint64_t first_base, uint64_t n, uint8_t *out, int sm_count,
                         cudaStream_t st);
 
+int dp_short_occupancy_local(int G, int minb);
+void dp_short_launch_local(int G, int minb, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
+int dp_short_occupancy_global(int G, int minb, bool free_ends);
+void dp_short_launch_global(int G, int minb, bool free_ends, int grid, cudaStream_t st, const DpLaunch &L,
+                            const DpParams &P);
+
+int dp_short_occupancy(int G, int minb, int mode)
+{
+    return mode == M_LOCAL ? dp_short_occupancy_local(G, minb) : dp_short_occupancy_global(G, minb, mode == M_GLOBAL_FREE);
+}
+
+void dp_short_launch(int G, int minb, int mode, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
+{
+    if (mode == M_LOCAL) dp_short_launch_local(G, minb, grid, st, L, P);
+    else dp_short_launch_global(G, minb, mode == M_GLOBAL_FREE, grid, st, L, P);
+}
+
 int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
 {
     if (variant == 1) return dp_occupancy_v1(lanes16, gen, mode);
@@ -278,17 +313,34 @@ namespace {
 // Resident blocks per SM of every DP kernel, queried once outside any stream capture.
 void warm_occupancy()
 {
-    for (int v = 0; v < kVariants; ++v)
+    for (int v = 0; v < kShortVariant; ++v)
         for (int mode = 0; mode < 3; ++mode) {
             dp_occupancy(v, true, false, mode);
             dp_occupancy(v, false, false, mode);
             dp_occupancy(v, false, true, mode);
         }
+    for (int g = 4; g <= 32; g *= 2)
+        for (int minb = 2; minb <= 3; ++minb)
+            for (int mode = 0; mode < 3; ++mode) dp_short_occupancy(g, minb, mode);
 }
 
 void launch_class(pa_ctx *c, int slot, int mode, bool lanes16, bool gen, const DpLaunch &L, const DpParams &P)
 {
-    const int v = c->variant[slot];
+    int v = c->variant[slot];
+    if (v >= kShortVariant) {
+        // the short-pair kernel covers s16x2 lanes with unitary scores in the plain modes and
+        // groups of 4..32 lanes; anything else takes the default dp_kernel form
+        if (lanes16 && !gen && mode <= M_GLOBAL_FREE && dp_short_supports(L.G) && L.slots) {
+            const int minb = v == kShortVariant ? 2 : 3;
+            int per_sm = dp_short_occupancy(L.G, minb, mode);
+            if (c->opt.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)c->opt.blocks_per_sm);
+            c->grid[slot] = per_sm * c->sm_count;
+            dp_short_launch(L.G, minb, mode, c->grid[slot], c->stream, L, P);
+            c->last_launches++;
+            return;
+        }
+        v = mode == M_LOCAL ? 7 : 4;
+    }
     int per_sm = dp_occupancy(v, lanes16, gen, mode);
     if (c->opt.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)c->opt.blocks_per_sm);
     c->grid[slot] = per_sm * c->sm_count;
@@ -298,7 +350,8 @@ void launch_class(pa_ctx *c, int slot, int mode, bool lanes16, bool gen, const D
 
 // Classify, bucket and sort the pairs (steps 1-3); no host sync.
 pa_status enqueue_prep(pa_ctx *c, const DpParams &P, const ClassCfg &C, const uint8_t *s1, const uint64_t *o1,
-                       const uint8_t *s2, const uint64_t *o2, pa_result *out, uint64_t n_pairs)
+                       uint64_t b1, const uint8_t *s2, const uint64_t *o2, uint64_t b2, pa_result *out,
+                       uint64_t n_pairs)
 {
     cudaStream_t st = c->stream;
     PA_CUDA(c, cudaMemsetAsync(c->hist.p, 0, sizeof(uint32_t) * kBuckets, st));
@@ -306,7 +359,7 @@ pa_status enqueue_prep(pa_ctx *c, const DpParams &P, const ClassCfg &C, const ui
     PA_CUDA(c, cudaMemsetAsync(c->pstats.p, 0, sizeof(PrepStats), st));
     int cls_blocks = (int)std::min<uint64_t>((n_pairs * 32 + 127) / 128, (uint64_t)c->sm_count * 128);
     if (cls_blocks < 1) cls_blocks = 1;
-    k_classify<<<cls_blocks, 128, 0, st>>>(s1, o1, s2, o2, n_pairs, P, C, (uint32_t *)c->keys.p,
+    k_classify<<<cls_blocks, 128, 0, st>>>(s1, o1, b1, s2, o2, b2, n_pairs, P, C, (uint32_t *)c->keys.p,
                                               (uint32_t *)c->hist.p, (uint32_t *)c->qtab.p, out,
                                               (PrepStats *)c->pstats.p);
     k_scan_blocks<<<kBuckets / 1024, 1024, 0, st>>>((uint32_t *)c->hist.p, (uint32_t *)c->starts.p,
@@ -317,7 +370,7 @@ pa_status enqueue_prep(pa_ctx *c, const DpParams &P, const ClassCfg &C, const ui
     const int sc_blocks = (int)std::max<uint64_t>(1, (n_pairs + kBlock - 1) / kBlock);
     k_scatter<<<sc_blocks, kBlock, 0, st>>>((uint32_t *)c->keys.p, n_pairs, (uint32_t *)c->cursor.p,
                                             (uint32_t *)c->order.p, (uint32_t *)c->ranges.p,
-                                            (uint32_t *)c->counts.p);
+                                            (uint32_t *)c->counts.p, (const PrepStats *)c->pstats.p, out);
     c->last_launches += 6;
     PA_CUDA(c, cudaGetLastError());
     return PA_OK;
@@ -325,14 +378,14 @@ pa_status enqueue_prep(pa_ctx *c, const DpParams &P, const ClassCfg &C, const ui
 
 // Everything between inputs-on-device and results-on-device; no host sync.
 pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const ClassCfg &C, const uint8_t *s1,
-                  const uint64_t *o1, uint64_t b1, const uint8_t *s2, const uint64_t *o2, pa_result *out,
-                  uint64_t n_pairs)
+                  const uint64_t *o1, uint64_t b1, const uint8_t *s2, const uint64_t *o2, uint64_t b2,
+                  pa_result *out, uint64_t n_pairs)
 {
     cudaStream_t st = c->stream;
     // counters: [0..3] group queues, [4] rerun count, [5] zero, [6] long rerun count, [8] error
     // bits, [9..12] CTA queues, [13..15] cluster queues, [16..21] routing of the largest pairs
     uint32_t *counters = (uint32_t *)c->counters.p;
-    pa_status ps = enqueue_prep(c, P, C, s1, o1, s2, o2, out, n_pairs);
+    pa_status ps = enqueue_prep(c, P, C, s1, o1, b1, s2, o2, b2, out, n_pairs);
     if (ps) return ps;
     const int cl_grid = c->ring.p ? dp_cluster_grid(true, false, P.local ? M_LOCAL : M_GLOBAL, c->ring_grid) : 0;
     if (c->ring.p) {
@@ -349,6 +402,8 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
     L.order = (const uint32_t *)c->order.p;
     L.out = out;
     L.boundary = (Cell *)c->boundary.p;
+    L.slots = (Slot *)c->slots.p;
+    L.spin_limit = c->wait_limit;
     L.rerun_list = (uint32_t *)c->rerun.p;
     L.rerun_count = counters + 4;
     if (C.rank_map) {
@@ -497,6 +552,7 @@ pa_status prepare_buffers(pa_ctx *c, uint64_t n_pairs, uint64_t b1)
     if ((s = ensure(c, c->pstats, sizeof(PrepStats)))) return s;
     if ((s = ensure(c, c->qtab, (b1 + np) * 4))) return s;
     if ((s = ensure(c, c->boundary, (b1 + np) * sizeof(Cell)))) return s;
+    if ((s = ensure(c, c->slots, (b1 + np) * sizeof(Slot)))) return s;
     return PA_OK;
 }
 
@@ -600,7 +656,18 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     PA_CUDA(c, cudaEventRecord(c->ev0, st));
     PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, st));
     PA_CUDA(c, cudaMemsetAsync(c->band_ctr.p, 0, 256, st));
-    if ((s = enqueue_prep(c, P, C, s1, o1, s2, o2, out, np))) return s;
+    if ((s = enqueue_prep(c, P, C, s1, o1, b1, s2, o2, b2, out, np))) return s;
+    {
+        // the classifier checked the offsets; a batch with inconsistent ones is not aligned (and
+        // the band features, which read the sequences, must not run on it)
+        unsigned long long bad = 0;
+        PA_CUDA(c, cudaMemcpyAsync(&bad, &((PrepStats *)c->pstats.p)->bad_offsets, sizeof(bad),
+                                   cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaStreamSynchronize(st));
+        if (bad)
+            return fail(c, PA_ERR_INVALID_ARGUMENT,
+                        "offsets decrease or run past seq1_bytes / seq2_bytes; no pair was aligned");
+    }
     BandSpec *spec = (BandSpec *)c->band_spec.p;
     if (h_bands) {
         if ((s = ensure(c, c->band_in, np * 40))) return s;
@@ -629,6 +696,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     L.qtab = (const uint32_t *)c->qtab.p;
     L.out = out;
     L.boundary = (Cell *)c->boundary.p;
+    L.slots = (Slot *)c->slots.p;
     L.band_win = (const int2 *)c->band_win.p;
     L.band = spec;
     L.band_code = (uint8_t *)c->band_code.p;
@@ -636,6 +704,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     L.ring = (Cell *)c->ring.p;
     L.ring_stride = (uint64_t)c->ring_m + 2;
     L.error = counters + 8;
+    L.spin_limit = c->wait_limit;
     // the full DP of a list: group kernels (with the s16 -> s32 redo list), whole blocks or clusters
     auto full_dp = [&](int k, const uint32_t *list, uint32_t *count_word, uint32_t *queue) -> pa_status {
         DpLaunch F = L;
@@ -865,6 +934,9 @@ pa_status read_stats(pa_ctx *c, pa_stats *stats)
         stats->pairs_trivial = ps.n_class[K_NONE];
         stats->pairs_rerun = rr;
     }
+    if (ps.bad_offsets)
+        return fail(c, PA_ERR_INVALID_ARGUMENT,
+                    "offsets decrease or run past seq1_bytes / seq2_bytes; no pair was aligned");
     if (ctr[8]) return fail(c, PA_ERR_TIMEOUT, "a CTA-mode progress wait ran out");
     if (ps.overflow) return fail(c, PA_ERR_OVERFLOW, "scores of some pairs could exceed int32");
     if (ps.invalid) return fail(c, PA_ERR_INVALID_ARGUMENT, "a sequence holds a symbol outside the substitution matrix");
@@ -899,11 +971,21 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
         key.ptrs[0] = s1; key.ptrs[1] = o1; key.ptrs[2] = s2; key.ptrs[3] = o2; key.ptrs[4] = out;
         key.ptrs[5] = c->boundary.p;
         key.n_pairs = n_pairs; key.b1 = b1; key.b2 = b2; key.cfg = *cfg;
+        for (int k = 0; k < 3; ++k) { key.G[k] = c->G[k]; key.variant[k] = c->variant[k]; }
+        key.wait_limit = c->wait_limit;
         auto it = c->graphs.find(key);
         if (it == c->graphs.end()) {
+            if (c->graphs.size() >= kMaxGraphs) {
+                // a caller that rotates buffers would otherwise keep one graph per buffer set
+                auto lru = c->graphs.begin();
+                for (auto g = c->graphs.begin(); g != c->graphs.end(); ++g)
+                    if (g->second.last_use < lru->second.last_use) lru = g;
+                cudaGraphExecDestroy(lru->second.exec);
+                c->graphs.erase(lru);
+            }
             cudaGraph_t g;
             PA_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            pa_status es = enqueue(c, cfg, P, C, s1, o1, b1, s2, o2, out, n_pairs);
+            pa_status es = enqueue(c, cfg, P, C, s1, o1, b1, s2, o2, b2, out, n_pairs);
             cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
             if (es) return es;
             if (ce != cudaSuccess) return fail(c, PA_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
@@ -911,13 +993,14 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
             ce = cudaGraphInstantiate(&ex, g, 0);
             cudaGraphDestroy(g);
             if (ce != cudaSuccess) return fail(c, PA_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ce));
-            it = c->graphs.emplace(key, ex).first;
+            it = c->graphs.emplace(key, GraphEntry{ex, 0}).first;
         } else {
             c->last_launches = 6 + 3 + (P.local ? 0 : 1) + (c->ring.p ? (P.local ? 7 : 8) + (C.team_max_n > 0 ? 3 : 0) : 0);
         }
-        PA_CUDA(c, cudaGraphLaunch(it->second, c->stream));
+        it->second.last_use = ++c->graph_clock;
+        PA_CUDA(c, cudaGraphLaunch(it->second.exec, c->stream));
     } else {
-        if ((s = enqueue(c, cfg, P, C, s1, o1, b1, s2, o2, out, n_pairs))) return s;
+        if ((s = enqueue(c, cfg, P, C, s1, o1, b1, s2, o2, b2, out, n_pairs))) return s;
     }
     PA_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     if (stats) {
@@ -1051,9 +1134,9 @@ pa_status pa_destroy(pa_ctx *c)
     if (!c) return PA_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    drop_graphs(c);
     DevBuf *bufs[] = {&c->keys, &c->order, &c->hist, &c->starts, &c->cursor, &c->sums, &c->ranges,
-                      &c->counts, &c->qtab, &c->boundary, &c->rerun, &c->counters, &c->pstats,
+                      &c->counts, &c->qtab, &c->boundary, &c->slots, &c->rerun, &c->counters, &c->pstats,
                       &c->in_seq1, &c->in_off1, &c->in_seq2, &c->in_off2, &c->in_out,
                       &c->band_spec, &c->band_win, &c->band_code, &c->band_bsum, &c->band_ctr, &c->band_in,
                       &c->mlp_feat, &c->mlp_x, &c->mlp_h1, &c->mlp_h2, &c->mlp_out,
@@ -1135,8 +1218,14 @@ pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells)
 {
     if (!ctx) return PA_ERR_INVALID_ARGUMENT;
     ctx->long_cells = cells > (uint64_t)INT64_MAX ? INT64_MAX : (int64_t)std::max<uint64_t>(cells, 1);
-    for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);   // the classifier's rule changed
-    ctx->graphs.clear();
+    drop_graphs(ctx);   // the classifier's rule changed
+    return PA_OK;
+}
+
+pa_status pa_set_wait_limit(pa_ctx *ctx, uint32_t polls)
+{
+    if (!ctx) return PA_ERR_INVALID_ARGUMENT;
+    ctx->wait_limit = polls;
     return PA_OK;
 }
 
@@ -1144,8 +1233,7 @@ pa_status pa_set_team_threshold(pa_ctx *ctx, uint32_t max_rows)
 {
     if (!ctx) return PA_ERR_INVALID_ARGUMENT;
     ctx->team_max_n = (int32_t)std::min<uint32_t>(max_rows, 1u << 30);
-    for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
-    ctx->graphs.clear();
+    drop_graphs(ctx);
     return PA_OK;
 }
 
@@ -1154,8 +1242,7 @@ pa_status pa_set_cluster_threshold(pa_ctx *ctx, uint64_t cells, uint32_t min_row
     if (!ctx) return PA_ERR_INVALID_ARGUMENT;
     ctx->huge_cells = cells > (uint64_t)INT64_MAX ? INT64_MAX : (int64_t)std::max<uint64_t>(cells, 1);
     ctx->huge_min_n = (int32_t)std::min<uint32_t>(std::max<uint32_t>(min_rows, 1), 1u << 30);
-    for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
-    ctx->graphs.clear();
+    drop_graphs(ctx);
     return PA_OK;
 }
 
@@ -1191,8 +1278,7 @@ pa_status pa_set_substitution_matrix(pa_ctx *ctx, const uint8_t *symbols, uint32
     ctx->mat_dim = (int32_t)dim;
     ctx->mat_max = hi;
     ctx->mat_min = lo;
-    for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);   // they hold the old dim
-    ctx->graphs.clear();
+    drop_graphs(ctx);   // they hold the old dim
     return PA_OK;
 }
 
@@ -1639,6 +1725,7 @@ pa_status pa_band_labels(pa_ctx *ctx, const pa_config *config, const uint8_t *se
             L.out = dout; L.boundary = dbound; L.G = 8;
             L.dump = ddump; L.dump_off = ddoff; L.labels = dlab;
             L.error = dctr + 4;
+            L.spin_limit = ctx->wait_limit;
             ok = cudaMemsetAsync(dctr, 0, 8, st) == cudaSuccess;
             if (ok && ns) band_labels_launch(rev == 1, grid, st, L, P);
             if (ok && !longs.empty()) {
@@ -1679,7 +1766,7 @@ pa_status pa_set_tuning(pa_ctx *ctx, const pa_tuning *t)
     for (int m = 0; m < 2; ++m)
         if (!valid_variant(t->variant_s16[m]) || !valid_variant(t->variant_s32[m]) || !valid_G(t->group_threads_s16[m]) ||
             !valid_G(t->group_threads_s32[m]))
-            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "tuning: variant must be 0..8 and group_threads 1..32, power of two");
+            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "tuning: variant must be 0..10 and group_threads 1..32, power of two");
     ctx->tuning = *t;
     ctx->fixed_G = ctx->fixed_variant = false;
     return PA_OK;

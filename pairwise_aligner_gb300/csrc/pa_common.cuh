@@ -43,6 +43,13 @@ struct __align__(8) Cell {
     uint32_t h, e;
 };
 
+// One streamed column of a short-pair unit (s16x2 lanes, pa_short.cuh): the score tables
+// of both lanes for the column's base and the top input of the current pass (H and the
+// downward gap of the row above the pass's first row).
+struct __align__(16) Slot {
+    uint32_t ta, tb, h, e;
+};
+
 // Band of one pair (band mode): the centre line runs through (0, 0), the 8
 // checkpoints (i_c, i_c + diag[c]) with i_c = (c + 1) * m / 9, and (m, n); the
 // half-width tapers linearly from w_start at column 0 to w_min at column m.
@@ -97,6 +104,11 @@ struct DpLaunch {
     const int8_t *rank_map;
     const int32_t *matrix;
     int32_t mdim;
+    // short-pair kernel (pa_short.cuh): (seq1_bytes + n_pairs) column slots, pair k's at off1[k] + k
+    Slot *slots;
+    // CTA / team / cluster modes: polls a progress wait makes after its first look before it
+    // gives up (pa_set_wait_limit; default 2^24)
+    uint32_t spin_limit;
 };
 
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)
@@ -111,6 +123,14 @@ __device__ __forceinline__ uint32_t dna_code(uint32_t b) { return ((b >> 1) ^ (b
 __device__ __forceinline__ bool dna_valid(uint32_t b)
 {
     return ((0x54474341u >> (8u * dna_code(b))) & 0xffu) == b;
+}
+
+// 4-byte score table of a streamed base: match in byte code(b), mismatch elsewhere;
+// a byte outside A/C/G/T matches nothing.
+__device__ __forceinline__ uint32_t score_table(uint32_t b, uint32_t match4, uint32_t mis4)
+{
+    if (!dna_valid(b)) return mis4;
+    return prmt(match4, mis4, 0x4444u ^ (4u << (4u * dna_code(b))));
 }
 
 // Border cell of the first row / column (affine_initialisation_strategy.hpp:38-51):

@@ -30,9 +30,10 @@
 //     hgap = VMAX(hgap - |ext|, Ho);  vgap = VMAX(vgap - |ext|, Ho)
 // s16x2 values are stored with a per-group offset K so that every halfword
 // stays in [0, 32767]: subtracting a constant never borrows across halfwords and
-// signed DPX comparisons stay valid.  Local: true 0 == K.  Global: the clamp at
-// 2048 is a floor; a result above floor + smax * min(m, n) cannot have been
-// influenced by a clamp and is exact, anything else is recomputed in s32.
+// signed DPX comparisons stay valid.  Local: true 0 == K.  Global modes store the
+// column-shifted H'(i, j) = H(i, j) - smax * i, which no step increases, and clamp it
+// at a floor (stored 2048): a cell that met the clamp stays at or below the floor, so a
+// result whose H' is above the floor is exact; anything else is recomputed in s32.
 //
 // Tracking (the reference trackers, tracker/*.hpp):
 //   local  -- running column maximum per strip; on a strict improvement the
@@ -153,6 +154,7 @@ struct GroupWork {
     int *prog_in, *prog_out;       // CTA mode: progress of the pass above / of this pass
     int32_t base_in, base_out;     // progress value of column 0 of those passes
     int32_t seen;                  // last progress value thread 0 observed
+    bool wait_failed;              // a progress wait of this unit ran out (thread 0 of a group)
     int32_t cs[2], ci[2], cj[2];   // candidate (score, end1, end2) per lane
     int32_t lb_v[8], lb_j[8];      // label mode: best forward + reverse score per checkpoint and its row
     // band mode: columns ibase+1 .. iend of the current pass; thread 0's first diagonal
@@ -164,8 +166,9 @@ struct GroupWork {
 
 // CTA mode: the groups of a block work on consecutive passes of one pair; the
 // group of pass p waits (thread 0, before reading boundary column c) until the
-// pass above has published column c.  Waits are bounded; a wait that runs out
-// sets an error bit and the kernel carries on (its result is reported invalid).
+// pass above has published column c.  Waits are bounded (DpLaunch::spin_limit polls
+// after the first look, default kSpinLimit); a wait that runs out sets an error bit,
+// the pair's result is written as an error (PA_RESULT_ERROR) and the kernel carries on.
 constexpr uint32_t kSpinLimit = 1u << 24;
 constexpr uint32_t kErrWaitTimeout = 1u;
 
@@ -184,12 +187,13 @@ __device__ __forceinline__ void store_release_cluster(int *p, int v)
 }
 
 template <int SCOPE>
-__device__ __forceinline__ int32_t wait_progress(int *flag, int32_t need, uint32_t *err)
+__device__ __forceinline__ int32_t wait_progress(int *flag, int32_t need, uint32_t *err, uint32_t limit)
 {
-    for (uint32_t it = 0; it < kSpinLimit; ++it) {
+    for (uint32_t it = 0;; ++it) {
         const int v = SCOPE == 2 ? load_acquire_cluster(flag)
                                  : cuda::atomic_ref<int, cuda::thread_scope_block>(*flag).load(cuda::memory_order_acquire);
         if (v >= need) return v;
+        if (it >= limit) break;
         if (it >= 64) __nanosleep(64);
     }
     if (err) atomicOr(err, kErrWaitTimeout);
@@ -355,7 +359,10 @@ __device__ __forceinline__ void run_pass(const DpLaunch &L, const DpParams &P, G
     // thread 0 of a pass below the first reads the boundary row; in CTA mode it first
     // waits until the pass above has published the column
     auto ready = [&](int32_t col) {
-        if (SYNC && w.seen < w.base_in + col) w.seen = wait_progress<SYNC>(w.prog_in, w.base_in + col, L.error);
+        if (SYNC && w.seen < w.base_in + col) {
+            w.seen = wait_progress<SYNC>(w.prog_in, w.base_in + col, L.error, L.spin_limit);
+            if (w.seen == INT32_MAX) w.wait_failed = true;
+        }
     };
     auto advance = [&](int32_t i) {                  // at column i < iend: fetch what column i + 1 needs
         if (PF2) {
@@ -629,6 +636,7 @@ __device__ __forceinline__ void init_work(const DpLaunch &L, const DpParams &P, 
     w.buf = L.boundary + (L.off1[owner] + owner);
     w.bin = w.bout = w.buf;
     w.seen = INT32_MIN;
+    w.wait_failed = false;
     if (NL == 2) {
         if (MODE == M_LOCAL) {
             w.Kt = 2048;
@@ -696,7 +704,10 @@ __device__ __forceinline__ void pass_body(const DpLaunch &L, const DpParams &P, 
         const int32_t c0 = bcur.x - 1;
         w.diag0 = NEGV;
         if (t == 0 && p > 0 && c0 >= bprev.x && c0 <= bprev.y) {
-            if (SYNC && w.seen < w.base_in + c0) w.seen = wait_progress<SYNC>(w.prog_in, w.base_in + c0, L.error);
+            if (SYNC && w.seen < w.base_in + c0) {
+                w.seen = wait_progress<SYNC>(w.prog_in, w.base_in + c0, L.error, L.spin_limit);
+                if (w.seen == INT32_MAX) w.wait_failed = true;
+            }
             w.diag0 = load_cell<SYNC>(w.bin + c0).h;
         }
     }
@@ -796,6 +807,18 @@ __device__ __forceinline__ void emit(const DpLaunch &L, const DpParams &P, Group
         r.flags = L.rerun ? PA_RESULT_RERUN : 0;
         r.band_rounds = 0;
         if (MODE == M_LOCAL && w.cs[l] <= 0) { r.end1 = 0; r.end2 = 0; }
+        if (w.wait_failed) {
+            // a boundary row was read before it was published: the score is not valid
+            r.score = INT32_MIN;
+            r.end1 = r.end2 = 0;
+            r.flags = PA_RESULT_ERROR;
+            L.out[w.id[l]] = r;
+            if (MODE == M_BAND) {
+                L.band_code[first + l] = 0;
+                if (L.band_ub) L.band_ub[w.id[l]] = INT32_MAX;
+            }
+            continue;
+        }
         if (MODE == M_BAND) {
             uint8_t code;
             if (NL == 2 && (int64_t)w.cs[l] - (int64_t)P.shift * w.ci[l] <= (int64_t)w.floor_true) {
@@ -879,6 +902,7 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cta(DpLaunch L, DpParams 
     __shared__ int32_t s_cand[NG][2][4];
     __shared__ int32_t s_lb[MODE == M_LABEL_REV ? NG : 1][8][2];
     __shared__ unsigned long long s_cells[NG];
+    __shared__ bool s_fail[NG];
     const int t = threadIdx.x & 31, g = threadIdx.x >> 5;
     const unsigned gmask = 0xffffffffu;
     const uint32_t count_main = *L.count_ptr;
@@ -927,10 +951,12 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cta(DpLaunch L, DpParams 
             if (MODE == M_LABEL_REV)
                 for (int c = 0; c < 8; ++c) { s_lb[g][c][0] = w.lb_v[c]; s_lb[g][c][1] = w.lb_j[c]; }
             s_cells[g] = w.cells;
+            s_fail[g] = w.wait_failed;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             for (int k = 1; k < NG; ++k) {
+                w.wait_failed |= s_fail[k];
                 for (int l = 0; l < 2; ++l) {
                     const int32_t *c = s_cand[k][l];
                     if (better(c[0], c[1], c[2], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = c[0]; w.ci[l] = c[1]; w.cj[l] = c[2]; }
@@ -970,6 +996,7 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_team(DpLaunch L, DpParams
     __shared__ int32_t s_cand[NW][2][4];
     __shared__ int32_t s_lb[MODE == M_LABEL_REV ? NW : 1][8][2];
     __shared__ unsigned long long s_cells[NW];
+    __shared__ bool s_fail[NW];
     // the unit lists, in shared memory so that they hold no registers during the passes
     __shared__ const uint32_t *s_order[2];
     __shared__ uint32_t s_count[2], s_units_lead, s_units;
@@ -1031,10 +1058,12 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_team(DpLaunch L, DpParams
             if (MODE == M_LABEL_REV)
                 for (int c = 0; c < 8; ++c) { s_lb[g][c][0] = w.lb_v[c]; s_lb[g][c][1] = w.lb_j[c]; }
             s_cells[g] = w.cells;
+            s_fail[g] = w.wait_failed;
         }
         team_sync();
         if (g % T == 0 && t == 0) {
             for (int k = g + 1; k < g + T; ++k) {
+                w.wait_failed |= s_fail[k];
                 for (int l = 0; l < 2; ++l) {
                     const int32_t *c = s_cand[k][l];
                     if (better(c[0], c[1], c[2], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = c[0]; w.ci[l] = c[1]; w.cj[l] = c[2]; }
@@ -1078,6 +1107,7 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cluster(DpLaunch L, DpPar
     __shared__ int32_t s_part[2][4];             // this block's merged result, read by rank 0
     __shared__ int32_t s_plb[8][2];
     __shared__ unsigned long long s_pcells;
+    __shared__ bool s_fail[NW], s_pfail;
     const int t = threadIdx.x & 31, g = threadIdx.x >> 5;
     const unsigned gmask = 0xffffffffu;
     const uint32_t count = *L.count_ptr;
@@ -1120,10 +1150,12 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cluster(DpLaunch L, DpPar
             }
             for (int c = 0; c < 8; ++c) { s_lb[g][c][0] = w.lb_v[c]; s_lb[g][c][1] = w.lb_j[c]; }
             s_cells[g] = w.cells;
+            s_fail[g] = w.wait_failed;
         }
         __syncthreads();
         // merge the block's groups, then rank 0 merges the blocks
-        auto merge = [&](const int32_t (*cand)[4], const int32_t (*lb)[2], unsigned long long cells) {
+        auto merge = [&](const int32_t (*cand)[4], const int32_t (*lb)[2], unsigned long long cells, bool failed) {
+            w.wait_failed |= failed;
             for (int l = 0; l < 2; ++l) {
                 const int32_t *c = cand[l];
                 if (better(c[0], c[1], c[2], w.cs[l], w.ci[l], w.cj[l])) { w.cs[l] = c[0]; w.ci[l] = c[1]; w.cj[l] = c[2]; }
@@ -1136,7 +1168,7 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cluster(DpLaunch L, DpPar
             w.cells += cells;
         };
         if (threadIdx.x == 0) {
-            for (int k = 1; k < NW; ++k) merge(s_cand[k], s_lb[k], s_cells[k]);
+            for (int k = 1; k < NW; ++k) merge(s_cand[k], s_lb[k], s_cells[k], s_fail[k]);
             for (int l = 0; l < 2; ++l) {
                 s_part[l][0] = w.cs[l];
                 s_part[l][1] = w.ci[l];
@@ -1145,12 +1177,13 @@ __global__ void __launch_bounds__(kBlock, 2) dp_kernel_cluster(DpLaunch L, DpPar
             }
             for (int c = 0; c < 8; ++c) { s_plb[c][0] = w.lb_v[c]; s_plb[c][1] = w.lb_j[c]; }
             s_pcells = w.cells;
+            s_pfail = w.wait_failed;
         }
         cluster.sync();
         if (rank == 0 && threadIdx.x == 0) {
             for (int r = 1; r < CL; ++r)
                 merge(cluster.map_shared_rank(s_part, r), cluster.map_shared_rank(s_plb, r),
-                      *cluster.map_shared_rank(&s_pcells, r));
+                      *cluster.map_shared_rank(&s_pcells, r), *cluster.map_shared_rank(&s_pfail, r));
             emit<V, MODE>(L, P, w, first);
         }
         cluster.sync();

@@ -30,7 +30,20 @@ struct PrepStats {
     unsigned long long n_class[16];
     unsigned long long overflow;    // pairs whose int32 bound fails
     unsigned long long invalid;     // substitution-matrix scoring: pairs with a symbol outside it
+    unsigned long long bad_offsets; // pairs whose offsets are decreasing or run past the byte buffers
 };
+
+// Result of a pair the DP does not compute (no valid score): INT32_MIN at (0, 0).
+__device__ __forceinline__ pa_result error_result(uint8_t flags)
+{
+    pa_result r;
+    r.score = INT32_MIN;
+    r.end1 = r.end2 = 0;
+    r.width = 32;
+    r.flags = flags;
+    r.band_rounds = 0;
+    return r;
+}
 
 __device__ __forceinline__ uint32_t quant_len(uint32_t m)
 {
@@ -44,14 +57,6 @@ __device__ __forceinline__ uint32_t quant_shape(uint32_t s)
     if (s < 32u) return s;
     const uint32_t e = 31u - __clz(s);
     return min(63u, 32u + (e - 5u) * 4u + ((s >> (e - 2u)) & 3u));
-}
-
-// 4-byte score table of a streamed base: match in byte code(b), mismatch elsewhere;
-// a byte outside A/C/G/T matches nothing.
-__device__ __forceinline__ uint32_t score_table(uint32_t b, uint32_t match4, uint32_t mis4)
-{
-    if (!dna_valid(b)) return mis4;
-    return prmt(match4, mis4, 0x4444u ^ (4u << (4u * dna_code(b))));
 }
 
 // Result of a pair with an empty sequence (no DP needed); same candidate rules as the DP.
@@ -72,10 +77,14 @@ __device__ void trivial_result(const DpParams &P, int32_t m, int32_t n, pa_resul
     r.score = s; r.end1 = i; r.end2 = j;
 }
 
-// One warp per pair: check sequence2's alphabet, pick the class, write the bucket
-// key, the score tables of sequence1 and the trivial results.
-__global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__restrict__ off1,
-                           const uint8_t *__restrict__ seq2, const uint64_t *__restrict__ off2,
+// One warp per pair: check the pair's offsets against the byte buffers and sequence2's
+// alphabet, pick the class, write the bucket key, the score tables of sequence1 and the
+// results of pairs the DP does not compute: empty sequences (their border result),
+// inconsistent offsets, scores that could exceed int32 and, with a substitution matrix,
+// symbols outside it (INT32_MIN and a PA_RESULT_* flag).  Sequence bytes and scratch
+// indices are touched only for pairs whose offsets passed the check.
+__global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__restrict__ off1, uint64_t seq1_bytes,
+                           const uint8_t *__restrict__ seq2, const uint64_t *__restrict__ off2, uint64_t seq2_bytes,
                            uint64_t n_pairs, DpParams P, ClassCfg C, uint32_t *__restrict__ keys,
                            uint32_t *__restrict__ hist, uint32_t *__restrict__ qtab, pa_result *__restrict__ out,
                            PrepStats *__restrict__ st)
@@ -86,10 +95,18 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
     const uint32_t match4 = (uint8_t)(P.match - P.shift) * 0x01010101u;     // scores of H - shift * column
     const uint32_t mis4 = (uint8_t)(P.mismatch - P.shift) * 0x01010101u;
     // statistics are summed per lane 0 and per block, then added once per block
-    unsigned long long my_cells = 0, my_class[16] = {}, my_overflow = 0;
+    unsigned long long my_cells = 0, my_class[16] = {}, my_overflow = 0, my_bad = 0;
     for (uint64_t p = warp; p < n_pairs; p += nwarps) {
-        const uint64_t q0 = off1[p], t0 = off2[p];
-        const int64_t m = (int64_t)(off1[p + 1] - q0), n = (int64_t)(off2[p + 1] - t0);
+        const uint64_t q0 = off1[p], q1 = off1[p + 1], t0 = off2[p], t1 = off2[p + 1];
+        if (q0 > q1 || q1 > seq1_bytes || t0 > t1 || t1 > seq2_bytes) {
+            if (lane == 0) {
+                out[p] = error_result(PA_RESULT_ERROR);
+                keys[p] = (uint32_t)K_NONE << kClassShift;
+                ++my_bad;
+            }
+            continue;
+        }
+        const int64_t m = (int64_t)(q1 - q0), n = (int64_t)(t1 - t0);
         bool dna = true;
         for (int64_t j = 4 * lane; j < n; j += 128) {     // four independent loads per lane
             const uint8_t *q = seq2 + t0 + j;
@@ -100,12 +117,26 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
             if (left > 3) dna &= dna_valid(q[3]);
         }
         dna = __all_sync(0xffffffffu, dna);
+        bool symbols_ok = true;
         if (C.rank_map) {                                 // every symbol needs a rank
-            bool ok = true;
-            for (int64_t j = lane; j < n; j += 32) ok &= C.rank_map[seq2[t0 + j]] >= 0;
-            for (int64_t i = lane; i < m; i += 32) ok &= C.rank_map[seq1[q0 + i]] >= 0;
-            ok = __all_sync(0xffffffffu, ok);
-            if (!ok && lane == 0) atomicAdd(&st->invalid, 1ull);
+            for (int64_t j = lane; j < n; j += 32) symbols_ok &= C.rank_map[seq2[t0 + j]] >= 0;
+            for (int64_t i = lane; i < m; i += 32) symbols_ok &= C.rank_map[seq1[q0 + i]] >= 0;
+            symbols_ok = __all_sync(0xffffffffu, symbols_ok);
+            if (!symbols_ok && lane == 0) atomicAdd(&st->invalid, 1ull);
+        }
+        const int64_t sa = P.match < 0 ? -(int64_t)P.match : P.match;
+        const int64_t sb = P.mismatch < 0 ? -(int64_t)P.mismatch : P.mismatch;
+        const int64_t go = -(int64_t)P.gap_open, ge = -(int64_t)P.gap_ext;
+        const bool overflow =
+            (sa + sb) * min(m, n) + (go + ge) * (m + n + 2) + 2 * go + (int64_t)P.shift * (m + n) >= (1ll << 30);
+        if (m > 0 && n > 0 && (overflow || !symbols_ok)) {
+            // no DP: the pair's scores could exceed int32, or a symbol has no rank
+            if (lane == 0) {
+                out[p] = error_result(overflow ? PA_RESULT_OVERFLOW : PA_RESULT_ERROR);
+                keys[p] = (uint32_t)K_NONE << kClassShift;
+                if (overflow) ++my_overflow;
+            }
+            continue;
         }
         uint32_t klass;
         if (m == 0 || n == 0) klass = K_NONE;
@@ -130,11 +161,6 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
             }
         }
         if (lane == 0) {
-            const int64_t a = P.match < 0 ? -(int64_t)P.match : P.match;
-            const int64_t b = P.mismatch < 0 ? -(int64_t)P.mismatch : P.mismatch;
-            const int64_t o = -(int64_t)P.gap_open, e = -(int64_t)P.gap_ext;
-            const int64_t bound = (a + b) * min(m, n) + (o + e) * (m + n + 2) + 2 * o + (int64_t)P.shift * (m + n);
-            if (bound >= (1ll << 30)) ++my_overflow;
             uint32_t key;
             if (klass == K_NONE) {
                 pa_result r;
@@ -156,14 +182,15 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
             ++my_class[klass];
         }
     }
-    __shared__ unsigned long long sh[18];
-    if (threadIdx.x < 18) sh[threadIdx.x] = 0;
+    __shared__ unsigned long long sh[19];
+    if (threadIdx.x < 19) sh[threadIdx.x] = 0;
     __syncthreads();
     if (lane == 0) {
         if (my_cells) atomicAdd(&sh[0], my_cells);
         for (int k = 0; k < 16; ++k)
             if (my_class[k]) atomicAdd(&sh[1 + k], my_class[k]);
         if (my_overflow) atomicAdd(&sh[17], my_overflow);
+        if (my_bad) atomicAdd(&sh[18], my_bad);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -171,6 +198,7 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
         for (int k = 0; k < 16; ++k)
             if (sh[1 + k]) atomicAdd(&st->n_class[k], sh[1 + k]);
         if (sh[17]) atomicAdd(&st->overflow, sh[17]);
+        if (sh[18]) atomicAdd(&st->bad_offsets, sh[18]);
     }
 }
 
@@ -232,16 +260,24 @@ __global__ void k_scan_add(uint32_t *__restrict__ starts, uint32_t *__restrict__
     if ((x & ((1u << kClassShift) - 1u)) == 0u) ranges[x >> kClassShift] = s;   // class begin
 }
 
+// A batch with inconsistent offsets is not aligned at all: the pairs' scratch regions
+// (at off1[k] + k) could overlap when the offsets decrease somewhere, so every class is
+// left empty and every pair gets an error result.
 __global__ void k_scatter(const uint32_t *__restrict__ keys, uint64_t n_pairs, uint32_t *__restrict__ cursor,
                           uint32_t *__restrict__ order, const uint32_t *__restrict__ ranges,
-                          uint32_t *__restrict__ counts)
+                          uint32_t *__restrict__ counts, const PrepStats *__restrict__ st, pa_result *__restrict__ out)
 {
     const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const bool bad = st->bad_offsets != 0;
     if (p == 0) {
         // class sizes from the class begins (classes 7 and 11.. hold no keys)
-        for (int c = 0; c < kClasses; ++c) counts[c] = ranges[c + 1] - ranges[c];
+        for (int c = 0; c < kClasses; ++c) counts[c] = bad ? 0u : ranges[c + 1] - ranges[c];
     }
     if (p >= n_pairs) return;
+    if (bad) {
+        out[p] = error_result(PA_RESULT_ERROR);
+        return;
+    }
     const uint32_t key = keys[p];
     if ((key >> kClassShift) == K_NONE) return;
     const uint32_t pos = atomicAdd(&cursor[key], 1u);

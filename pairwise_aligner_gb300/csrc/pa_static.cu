@@ -29,7 +29,7 @@ constexpr int kStaticR = 16;
 static __device__ __align__(256) pa::Cell g_static_boundary[kStaticCells];
 static __device__ __align__(256) uint32_t g_static_counters[64];
 
-// Per device: the device addresses of the two arrays, looked up once.
+// Per device: the device addresses of the two arrays (see static_slot).
 struct StaticSlot {
     bool ready = false;
     pa::Cell *boundary = nullptr;
@@ -56,8 +56,11 @@ __device__ void empty_pair_result(const pa::DpParams &P, int32_t m, int32_t n, p
     r.score = s; r.end1 = i; r.end2 = j;
 }
 
+// A pair whose offsets decrease or run past the byte buffers is not aligned: its scratch
+// row (at off1[k] + k) could leave the static array.  It gets INT32_MIN and PA_RESULT_ERROR.
 template <int MODE>
-__global__ void __launch_bounds__(pa::kBlock, 2) dp_kernel_static(pa::DpLaunch L, pa::DpParams P, uint32_t count)
+__global__ void __launch_bounds__(pa::kBlock, 2) dp_kernel_static(pa::DpLaunch L, pa::DpParams P, uint32_t count,
+                                                                  uint64_t seq1_bytes, uint64_t seq2_bytes)
 {
     using namespace pa;
     using V = L32;
@@ -79,9 +82,26 @@ __global__ void __launch_bounds__(pa::kBlock, 2) dp_kernel_static(pa::DpLaunch L
         const uint32_t first = u * ppw + (uint32_t)g;
         if (first >= count) continue;
 
+        {
+            const uint64_t q0 = L.off1[first], q1 = L.off1[first + 1], t0 = L.off2[first], t1 = L.off2[first + 1];
+            if (q0 > q1 || q1 > seq1_bytes || t0 > t1 || t1 > seq2_bytes) {
+                if (t == 0) {
+                    pa_result r;
+                    r.score = INT32_MIN;
+                    r.end1 = r.end2 = 0;
+                    r.width = 32;
+                    r.flags = PA_RESULT_ERROR;
+                    r.band_rounds = 0;
+                    L.out[first] = r;
+                }
+                __syncwarp(gmask);
+                continue;
+            }
+        }
         GroupWork w;
         w.id[0] = w.id[1] = first;
         w.has_b = false;
+        w.wait_failed = false;
         w.qoff[0] = w.qoff[1] = L.off1[first];
         w.m[0] = w.m[1] = (int32_t)(L.off1[first + 1] - w.qoff[0]);
         w.toff[0] = w.toff[1] = L.off2[first];
@@ -171,16 +191,22 @@ __global__ void __launch_bounds__(pa::kBlock, 2) dp_kernel_static(pa::DpLaunch L
     }
 }
 
-// Device addresses of the static arrays on the current device; looked up on the
-// first call for that device (before any stream capture, see the header).
-pa_status static_slot(StaticSlot **out)
+// Device addresses of the static arrays on the current device.  Outside a stream capture
+// they are looked up again on every call (cudaGetSymbolAddress is a host-side lookup), so a
+// context that was reset and created again, which reloads this module at new addresses, is
+// followed; while `stream` is being captured the addresses of the last call on this device
+// are used, so the first call on a device must come before any capture.
+pa_status static_slot(cudaStream_t stream, StaticSlot **out)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return PA_ERR_NO_DEVICE; }
     if (dev < 0 || dev >= kMaxDevices) return PA_ERR_UNSUPPORTED;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) { cudaGetLastError(); return PA_ERR_CUDA; }
     std::lock_guard<std::mutex> lock(g_slots_mutex);
     StaticSlot &s = g_slots[dev];
-    if (!s.ready) {
+    if (cap != cudaStreamCaptureStatusNone && !s.ready) return PA_ERR_UNSUPPORTED;
+    if (cap == cudaStreamCaptureStatusNone) {
         void *b = nullptr, *c = nullptr;
         if (cudaGetSymbolAddress(&b, g_static_boundary) != cudaSuccess ||
             cudaGetSymbolAddress(&c, g_static_counters) != cudaSuccess) {
@@ -210,9 +236,8 @@ extern "C" pa_status pa_align_batch_device_static(const pa_config *config, const
     if (n_pairs == 0) return PA_OK;
     if (!d_seq1 || !d_off1 || !d_seq2 || !d_off2 || !d_out) return PA_ERR_INVALID_ARGUMENT;
     if (n_pairs >= (1ull << 31) || seq1_bytes + n_pairs > kStaticCells) return PA_ERR_TOO_LARGE;
-    (void)seq2_bytes;
     StaticSlot *slot = nullptr;
-    const pa_status s = static_slot(&slot);
+    const pa_status s = static_slot((cudaStream_t)stream, &slot);
     if (s != PA_OK) return s;
 
     const bool local = config->method == PA_METHOD_LOCAL;
@@ -256,9 +281,9 @@ extern "C" pa_status pa_align_batch_device_static(const pa_config *config, const
     const int grid = 2 * sms;
     const uint32_t count = (uint32_t)n_pairs;
     const int mode = local ? M_LOCAL : ((P.last_column_free || P.last_row_free) ? M_GLOBAL_FREE : M_GLOBAL);
-    if (mode == M_LOCAL) dp_kernel_static<M_LOCAL><<<grid, kBlock, 0, st>>>(L, P, count);
-    else if (mode == M_GLOBAL) dp_kernel_static<M_GLOBAL><<<grid, kBlock, 0, st>>>(L, P, count);
-    else dp_kernel_static<M_GLOBAL_FREE><<<grid, kBlock, 0, st>>>(L, P, count);
+    if (mode == M_LOCAL) dp_kernel_static<M_LOCAL><<<grid, kBlock, 0, st>>>(L, P, count, seq1_bytes, seq2_bytes);
+    else if (mode == M_GLOBAL) dp_kernel_static<M_GLOBAL><<<grid, kBlock, 0, st>>>(L, P, count, seq1_bytes, seq2_bytes);
+    else dp_kernel_static<M_GLOBAL_FREE><<<grid, kBlock, 0, st>>>(L, P, count, seq1_bytes, seq2_bytes);
     if (cudaGetLastError() != cudaSuccess) return PA_ERR_CUDA;
     return PA_OK;
 }
