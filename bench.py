@@ -21,6 +21,14 @@ One step = one call of the hot path over the whole batch:
             (pa_measure_roofline); HBM traffic against MEASURED_PEAKS.json.
   cpu_baseline -- the oracle's inter-sequence SIMD port on all host cores, on a
             bounded sample of the batch (rank 0 only).
+  exact  -- after the timed region, every result of the batch (score and both end
+            positions) compared with the scalar oracle on all host cores; the oracle is
+            the checker here, never the thing timed (rank 0; a seeded sample when the
+            batch is too large for the oracle to finish in about a minute).
+  learned_band -- band mode 1 (the shipped predictor) against the plain full DP on the
+            16,384 held-out pairs of the learned-band workload and on a 65,536-pair
+            sample of the mixed global stream: GCUPS of both, certified pairs, band
+            rounds, and whether the banded scores equal the plain ones.
 
 --impl reference times the CPU implementation of the path (the reference's own
 build when present, else the oracle's SIMD port) on the host cores.
@@ -384,6 +392,10 @@ def our_arm(args):
     if args.band:
         line["band"] = {k: st[k] for k in ("pairs_banded", "pairs_full_dp", "band_cells", "band_rounds")}
         line["band"]["options"] = ctx.band_options()
+    if rank == 0 and not args.no_exact:
+        line["exact"] = check_exact(d, res)
+    if rank == 0 and world == 1 and args.workload == "config2" and not args.no_band_section:
+        line["learned_band"] = learned_band_section(dev, stream, args)
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rate, npairs, dt = cpu_sample_rate(d, args.cpu_seconds, threads)
@@ -394,6 +406,92 @@ def our_arm(args):
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def check_exact(d: dict, res) -> dict:
+    """Every result of the batch against the scalar oracle (the checker, outside any timed
+    region): when the batch holds more than 3e10 cells, a seeded sample of 4,096 pairs."""
+    import numpy as np
+    from oracle import oracle as O
+    from pairwise_aligner_gb300 import workloads as W
+    n = len(d["off1"]) - 1
+    idx = np.arange(n)
+    if W.cells(d) > 3e10:
+        idx = np.sort(np.random.default_rng(99).choice(n, size=min(n, 4096), replace=False))
+    sub = W.subset(d, idx) if len(idx) < n else d
+    free = bool(d["local"])
+    oc = O.make_cfg(d["match"], d["mismatch"], d["gap_open"], d["gap_extension"], local=d["local"],
+                    first_column_free=free, first_row_free=free, last_column_free=free, last_row_free=free)
+    t0 = time.perf_counter()
+    sc, e1, e2 = O.align_batch(oc, sub["seq1"], sub["off1"], sub["seq2"], sub["off2"], nthreads=os.cpu_count())
+    r = res[idx]
+    same = bool(np.array_equal(r["score"], sc) and np.array_equal(r["end1"], e1) and np.array_equal(r["end2"], e2))
+    return {"equal": same, "pairs_checked": int(len(idx)), "of_pairs": int(n),
+            "against": "scalar oracle (oracle/pa_oracle.c), score + end1 + end2",
+            "seconds": round(time.perf_counter() - t0, 1)}
+
+
+def learned_band_section(dev, stream, args) -> dict:
+    """Band mode 1 with the shipped predictor against the plain DP on two global workloads."""
+    import numpy as np
+    import torch
+    import pairwise_aligner_gb300 as pa
+    from pairwise_aligner_gb300 import band as BD
+    from pairwise_aligner_gb300 import workloads as W
+    from pairwise_aligner_gb300.aligner import Aligner
+    out = {"model": "pairwise_aligner_gb300/data/band_model.npz", "unit": "GCUPS (full m*n cells per second)"}
+    model = BD.BandModel(device=dev)
+    model.load(BAND_MODEL)
+    for name, d in (("config4_eval_16384_pairs", W.config4(seed=424242, n_pairs=16384)),
+                    ("config5_sample_65536_pairs", W.config5(seed=515151, n_pairs=65536))):
+        cells = W.cells(d)
+        n = len(d["off1"]) - 1
+        s1 = torch.from_numpy(d["seq1"]).to(dev)
+        s2 = torch.from_numpy(d["seq2"]).to(dev)
+        o1 = torch.from_numpy(d["off1"].astype(np.int64)).to(dev)
+        o2 = torch.from_numpy(d["off2"].astype(np.int64)).to(dev)
+        entry = {"pairs": n, "cells": cells}
+        results = {}
+        for mode in (0, 1):
+            ctx = pa.Context(dev.index or 0)
+            if mode == 1:
+                model.to_context(ctx)
+            conf = dict(local=False, match=d["match"], mismatch=d["mismatch"], gap_open=d["gap_open"],
+                        gap_extension=d["gap_extension"], first_column_free=False, first_row_free=False,
+                        last_column_free=False, last_row_free=False, width_hint=0, band_mode=mode)
+            al = Aligner(conf, context=ctx)
+            out_t = torch.empty(n * 16, dtype=torch.uint8, device=dev)
+            for _ in range(2):
+                al.compute_device(s1, o1, s2, o2, out_t, stream=stream, stats=True)
+            torch.cuda.synchronize()
+            steps = 3
+            flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+            total = 0.0
+            for _ in range(steps):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                al.compute_device(s1, o1, s2, o2, out_t, stream=stream, stats=mode == 1)
+                b.record(stream)
+                b.synchronize()
+                total += a.elapsed_time(b)
+            ms = total / steps
+            results[mode] = np.frombuffer(out_t.cpu().numpy().tobytes(), dtype=pa.RESULT_DTYPE).copy()
+            key = "plain" if mode == 0 else "band"
+            entry[key] = {"gcups": round(cells / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 3)}
+            if mode == 1:
+                st = al.last_stats
+                entry[key].update(certified_pairs=int(st["pairs_banded"]), full_dp_pairs=int(st["pairs_full_dp"]),
+                                  band_cells=int(st["band_cells"]), rounds=int(st["band_rounds"]))
+            ctx.close()
+            del flush
+        entry["band_over_plain"] = round(entry["band"]["gcups"] / entry["plain"]["gcups"], 3)
+        entry["exact"] = bool(np.array_equal(results[0]["score"], results[1]["score"]))
+        out[name] = entry
+        del s1, s2, o1, o2
+    torch.cuda.empty_cache()
+    return out
 
 
 def input_kernels(dev, stream, ctx, n: int = 1 << 30, reps: int = 5) -> dict:
@@ -474,6 +572,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-input", action="store_true", help="skip the input-path kernel measurement")
+    ap.add_argument("--no-exact", action="store_true", help="skip the oracle check of the batch's results")
+    ap.add_argument("--no-band-section", action="store_true", help="skip the learned-band comparison")
     ap.add_argument("--traceback", action="store_true", help="also time pa_traceback_batch on the batch")
     ap.add_argument("--workload", choices=["config1", "config2", "config3", "config4", "config5"], default="config2")
     ap.add_argument("--band", type=int, choices=[0, 1, 2], default=0,

@@ -246,6 +246,11 @@ pa_status pa_mlp_to_bf16(const float *src, int rows, int cols, int ld_dst, void 
  * lanes; default 2^20.  1 sends every pair there, UINT64_MAX none. */
 pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells);
 
+/* Calls the context keeps captured as CUDA graphs (replayed when a call repeats the
+ * same buffers, sizes, configuration and launch shapes; at most 8, the least recently
+ * replayed is dropped first).  No counterpart in the reference. */
+pa_status pa_get_graph_count(const pa_ctx *ctx, uint32_t *out);
+
 /* Polls a CTA-mode progress wait makes after its first look before it gives up
  * (default 2^24, with a short sleep between polls).  A wait that gives up marks its
  * pair PA_RESULT_ERROR and the call returns PA_ERR_TIMEOUT; 0 gives up at the first

@@ -161,6 +161,7 @@ SIGNATURES = {
     "pa_set_cluster_threshold": ([_ctxp, ctypes.c_uint64, ctypes.c_uint32], ctypes.c_int),
     "pa_set_team_threshold": ([_ctxp, ctypes.c_uint32], ctypes.c_int),
     "pa_set_wait_limit": ([_ctxp, ctypes.c_uint32], ctypes.c_int),
+    "pa_get_graph_count": ([_ctxp, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
     "pa_set_band_options": ([_ctxp, ctypes.POINTER(PaBandOptions)], ctypes.c_int),
     "pa_get_band_options": ([_ctxp, ctypes.POINTER(PaBandOptions)], ctypes.c_int),
     "pa_set_band_model": ([_ctxp] + [ctypes.c_void_p] * 6, ctypes.c_int),

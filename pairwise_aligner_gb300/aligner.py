@@ -73,6 +73,12 @@ class Context:
         """Block-mode pairs whose sequence2 has at most `max_rows` rows run on 4-warp teams (0: none)."""
         _lib.check(self.lib.pa_set_team_threshold(self.ptr, int(max_rows)), self.ptr)
 
+    def graph_count(self) -> int:
+        """Calls this context keeps captured as CUDA graphs (at most 8)."""
+        n = ctypes.c_uint32()
+        _lib.check(self.lib.pa_get_graph_count(self.ptr, ctypes.byref(n)), self.ptr)
+        return n.value
+
     def set_wait_limit(self, polls: int):
         """Polls a CTA-mode progress wait makes before it gives up (default 2^24; 0: at the first look)."""
         _lib.check(self.lib.pa_set_wait_limit(self.ptr, int(polls)), self.ptr)

@@ -33,8 +33,8 @@ namespace {
 constexpr int kR = 16;             // rows per thread per lane
 constexpr int64_t kDefaultRingM = 65536;   // device entry points: CTA mode up to this sequence1 length
 constexpr int kDefaultG = 8;       // threads per group
-constexpr int kVariants = 11;      // inner-loop variants: 0..8 dp_kernel (pa_kern_v*.cu), 9 / 10 dp_short
-constexpr int kShortVariant = 9;   // dp_short (s16x2 unitary short pairs) at 2 resident blocks per SM; 10: at 3
+constexpr int kShortVariant = 9;   // variants 9, 10: dp_short (s16x2 unitary short pairs), 16 / 32 rows per thread
+constexpr int kVariants = kShortVariant + kShortFormCount;   // 0..8: dp_kernel (pa_kern_v*.cu)
 
 struct DevBuf {
     void *p = nullptr;
@@ -244,21 +244,21 @@ void pack_2bit_launch(const uint8_t *in, uint64_t n, uint32_t *words, unsigned l
 void unpack_2bit_launch(const uint32_t *words, uint64_t first_base, uint64_t n, uint8_t *out, int sm_count,
                         cudaStream_t st);
 
-int dp_short_occupancy_local(int G, int minb);
-void dp_short_launch_local(int G, int minb, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
-int dp_short_occupancy_global(int G, int minb, bool free_ends);
-void dp_short_launch_global(int G, int minb, bool free_ends, int grid, cudaStream_t st, const DpLaunch &L,
+int dp_short_occupancy_local(int G, int form);
+void dp_short_launch_local(int G, int form, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
+int dp_short_occupancy_global(int G, int form, bool free_ends);
+void dp_short_launch_global(int G, int form, bool free_ends, int grid, cudaStream_t st, const DpLaunch &L,
                             const DpParams &P);
 
-int dp_short_occupancy(int G, int minb, int mode)
+int dp_short_occupancy(int G, int form, int mode)
 {
-    return mode == M_LOCAL ? dp_short_occupancy_local(G, minb) : dp_short_occupancy_global(G, minb, mode == M_GLOBAL_FREE);
+    return mode == M_LOCAL ? dp_short_occupancy_local(G, form) : dp_short_occupancy_global(G, form, mode == M_GLOBAL_FREE);
 }
 
-void dp_short_launch(int G, int minb, int mode, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
+void dp_short_launch(int G, int form, int mode, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
 {
-    if (mode == M_LOCAL) dp_short_launch_local(G, minb, grid, st, L, P);
-    else dp_short_launch_global(G, minb, mode == M_GLOBAL_FREE, grid, st, L, P);
+    if (mode == M_LOCAL) dp_short_launch_local(G, form, grid, st, L, P);
+    else dp_short_launch_global(G, form, mode == M_GLOBAL_FREE, grid, st, L, P);
 }
 
 int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
@@ -320,8 +320,8 @@ void warm_occupancy()
             dp_occupancy(v, false, true, mode);
         }
     for (int g = 4; g <= 32; g *= 2)
-        for (int minb = 2; minb <= 3; ++minb)
-            for (int mode = 0; mode < 3; ++mode) dp_short_occupancy(g, minb, mode);
+        for (int form = 0; form < kShortFormCount; ++form)
+            for (int mode = 0; mode < 3; ++mode) dp_short_occupancy(g, form, mode);
 }
 
 void launch_class(pa_ctx *c, int slot, int mode, bool lanes16, bool gen, const DpLaunch &L, const DpParams &P)
@@ -331,11 +331,12 @@ void launch_class(pa_ctx *c, int slot, int mode, bool lanes16, bool gen, const D
         // the short-pair kernel covers s16x2 lanes with unitary scores in the plain modes and
         // groups of 4..32 lanes; anything else takes the default dp_kernel form
         if (lanes16 && !gen && mode <= M_GLOBAL_FREE && dp_short_supports(L.G) && L.slots) {
-            const int minb = v == kShortVariant ? 2 : 3;
-            int per_sm = dp_short_occupancy(L.G, minb, mode);
+            // the free-end-gap form keeps 16 rows per thread (32 do not fit its registers)
+            const int form = mode == M_GLOBAL_FREE ? 0 : v - kShortVariant;
+            int per_sm = dp_short_occupancy(L.G, form, mode);
             if (c->opt.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)c->opt.blocks_per_sm);
             c->grid[slot] = per_sm * c->sm_count;
-            dp_short_launch(L.G, minb, mode, c->grid[slot], c->stream, L, P);
+            dp_short_launch(L.G, form, mode, c->grid[slot], c->stream, L, P);
             c->last_launches++;
             return;
         }
@@ -1219,6 +1220,13 @@ pa_status pa_set_cta_threshold(pa_ctx *ctx, uint64_t cells)
     if (!ctx) return PA_ERR_INVALID_ARGUMENT;
     ctx->long_cells = cells > (uint64_t)INT64_MAX ? INT64_MAX : (int64_t)std::max<uint64_t>(cells, 1);
     drop_graphs(ctx);   // the classifier's rule changed
+    return PA_OK;
+}
+
+pa_status pa_get_graph_count(const pa_ctx *ctx, uint32_t *out)
+{
+    if (!ctx || !out) return PA_ERR_INVALID_ARGUMENT;
+    *out = (uint32_t)ctx->graphs.size();
     return PA_OK;
 }
 

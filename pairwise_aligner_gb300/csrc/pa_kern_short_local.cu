@@ -2,9 +2,9 @@
 #include "pa_kern_short.cuh"
 
 namespace pa {
-int dp_short_occupancy_local(int G, int minb) { return occ_short_gb<M_LOCAL>(G, minb); }
-void dp_short_launch_local(int G, int minb, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
+int dp_short_occupancy_local(int G, int form) { return occ_short_gb<M_LOCAL>(G, form); }
+void dp_short_launch_local(int G, int form, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
 {
-    go_short_gb<M_LOCAL>(G, minb, grid, st, L, P);
+    go_short_gb<M_LOCAL>(G, form, grid, st, L, P);
 }
 }  // namespace pa

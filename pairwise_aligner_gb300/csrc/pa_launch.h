@@ -13,10 +13,11 @@ void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStre
                const DpParams &P);
 
 // Short-pair kernel in s16x2 lanes with unitary DNA scores (pa_short.cuh): G in {4, 8, 16,
-// 32} lanes per group, registers held to minb (2 or 3) resident blocks per SM; L.slots must
+// 32} lanes per group, form 0 (16 rows of sequence2 per thread) or 1 (32 rows); L.slots must
 // hold seq1_bytes + n_pairs column slots.
-int dp_short_occupancy(int G, int minb, int mode);
-void dp_short_launch(int G, int minb, int mode, int grid, cudaStream_t stream, const DpLaunch &L, const DpParams &P);
+constexpr int kShortFormCount = 2;
+int dp_short_occupancy(int G, int form, int mode);
+void dp_short_launch(int G, int form, int mode, int grid, cudaStream_t stream, const DpLaunch &L, const DpParams &P);
 inline bool dp_short_supports(int G) { return G == 4 || G == 8 || G == 16 || G == 32; }
 
 // CTA mode (long pairs): whole blocks per pair; L.ring must hold grid * 8 rows of
