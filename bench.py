@@ -154,7 +154,18 @@ def workload_name(d: dict, workload: str, n: int) -> str:
     return f"{d.get('name', workload)}_{n}_pairs_{d['match']:+d}/{d['mismatch']:+d}/{d['gap_open']:+d}/{d['gap_extension']:+d}"
 
 
-def cpu_sample_rate(d, budget_s: float, threads: int):
+def lanes_label(counts) -> str:
+    """Which lane widths of the CPU port finished the sample's pairs."""
+    return (f"pairs finished in 16 byte lanes: {counts[0]}, 8 int16 lanes: {counts[1]}, "
+            f"4 int32 lanes: {counts[2]}")
+
+
+PORT_LABEL = ("oracle inter-sequence SIMD port (oracle/pa_oracle.c, pa_oracle_bytes.cpp), 16-byte vectors, "
+              "pthreads: local A/C/G/T pairs in 16 byte lanes (the reference's saturated int8 width), the "
+              "rest in 8 int16 / 4 int32 lanes")
+
+
+def cpu_sample_rate(d, budget_s: float, threads: int, counts=None):
     """Time the oracle's SIMD port on a leading sample of the batch sized to ~budget_s seconds."""
     import numpy as np
     from oracle import oracle as O
@@ -165,7 +176,7 @@ def cpu_sample_rate(d, budget_s: float, threads: int):
     while True:
         sub = W.subset(d, np.arange(n))
         t0 = time.perf_counter()
-        O.simd_batch(cfg, sub["seq1"], sub["off1"], sub["seq2"], sub["off2"], nthreads=threads)
+        O.simd_batch(cfg, sub["seq1"], sub["off1"], sub["seq2"], sub["off2"], nthreads=threads, counts=counts)
         dt = time.perf_counter() - t0
         if dt >= budget_s * 0.5 or n >= n_total:
             return W.cells(sub) / dt / 1e9, n, dt
@@ -181,7 +192,7 @@ def reference_arm(args):
     from pairwise_aligner_gb300 import workloads as W
     d, _ = load_workload(args.pairs, args.workload)
     threads = os.cpu_count() or 1
-    kind, label = "port", "oracle inter-sequence SIMD port, int16x8 / int32x4 lanes (oracle/pa_oracle.c), pthreads"
+    kind, label = "port", PORT_LABEL
     # one step = a bounded leading sample, sized so W + K steps take about two minutes
     per_step = max(0.5, min(5.0, 100.0 / max(1, args.steps + args.warmup)))
     rate, n, dt = cpu_sample_rate(d, per_step, threads)
@@ -190,16 +201,17 @@ def reference_arm(args):
     for _ in range(args.warmup):
         O.simd_batch(cfg, sub["seq1"], sub["off1"], sub["seq2"], sub["off2"], nthreads=threads)
     times = []
+    counts = [0, 0, 0]
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        O.simd_batch(cfg, sub["seq1"], sub["off1"], sub["seq2"], sub["off2"], nthreads=threads)
+        O.simd_batch(cfg, sub["seq1"], sub["off1"], sub["seq2"], sub["off2"], nthreads=threads, counts=counts)
         times.append(time.perf_counter() - t0)
     cells = W.cells(sub)
     value = cells * len(times) / sum(times) / 1e9
-    sample = f"first {n} of {len(d['off1']) - 1} pairs ({cells:.3g} cells) per step; {label}"
+    sample = f"first {n} of {len(d['off1']) - 1} pairs ({cells:.3g} cells) per step; {label}; {lanes_label(counts)}"
     line = {"impl": "reference", "metric": METRIC if d["local"] else METRIC_GLOBAL, "value": round(value, 3), "unit": "GCUPS", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16 lanes (int32 where needed)",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8 lanes (int16 / int32 where needed)",
             "data": "synthetic", "config": {"workload": workload_name(d, args.workload, len(d["off1"]) - 1),
                                             "pairs_per_step": n},
             "cpu_baseline": {"value": round(value, 3), "unit": "GCUPS", "cores": threads, "kind": kind,
@@ -398,9 +410,11 @@ def our_arm(args):
         line["learned_band"] = learned_band_section(dev, stream, args)
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rate, npairs, dt = cpu_sample_rate(d, args.cpu_seconds, threads)
+        counts = [0, 0, 0]
+        rate, npairs, dt = cpu_sample_rate(d, args.cpu_seconds, threads, counts)
         line["cpu_baseline"] = {"value": round(rate, 3), "unit": "GCUPS", "cores": threads, "kind": "port",
-                                "sample": f"first {npairs} pairs of the batch, {dt:.1f} s, oracle SIMD port (int16x8 / int32x4)"}
+                                "sample": f"first {npairs} pairs of the batch, {dt:.1f} s; {PORT_LABEL}; "
+                                          f"{lanes_label(counts)}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -18,6 +18,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SRC = os.path.join(_HERE, "pa_oracle.c")
+_SRC_BYTES = os.path.join(_HERE, "pa_oracle_bytes.cpp")
 _LIB = os.path.join(_HERE, "liboracle.so")
 _lock = threading.Lock()
 _lib = None
@@ -41,12 +42,19 @@ class OracleCfg(ctypes.Structure):
 
 
 def build(force: bool = False) -> str:
-    """Compile oracle/pa_oracle.c into oracle/liboracle.so (portable flags, no -march)."""
+    """Compile oracle/pa_oracle.c and pa_oracle_bytes.cpp into oracle/liboracle.so (portable
+    flags, no -march)."""
     with _lock:
-        if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):
-            cmd = ["gcc", "-O3", "-std=c11", "-Wall", "-Wextra", "-Wno-psabi", "-fPIC", "-shared",
-                   "-pthread", _SRC, "-o", _LIB + ".tmp"]
-            subprocess.check_call(cmd)
+        newest = max(os.path.getmtime(_SRC), os.path.getmtime(_SRC_BYTES))
+        if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < newest:
+            obj = _LIB + f".bytes{os.getpid()}.o"
+            warn = ["-Wall", "-Wextra", "-Wno-psabi", "-fPIC"]
+            subprocess.check_call(["g++", "-O3", "-std=c++17", *warn, "-c", _SRC_BYTES, "-o", obj])
+            try:
+                subprocess.check_call(["gcc", "-O3", "-std=c11", *warn, "-shared", "-pthread", _SRC, obj,
+                                       "-o", _LIB + ".tmp"])
+            finally:
+                os.remove(obj)
             os.replace(_LIB + ".tmp", _LIB)
     return _LIB
 
@@ -72,6 +80,9 @@ def lib():
         L.pa_oracle_simd_batch.argtypes = [ctypes.POINTER(OracleCfg), u8p, u64p, u8p, u64p, ctypes.c_uint64,
                                            i32p, ctypes.c_int]
         L.pa_oracle_simd_batch.restype = ctypes.c_int
+        L.pa_oracle_simd_batch_lanes.argtypes = [ctypes.POINTER(OracleCfg), u8p, u64p, u8p, u64p, ctypes.c_uint64,
+                                                 i32p, ctypes.c_int, ctypes.c_int, u64p]
+        L.pa_oracle_simd_batch_lanes.restype = ctypes.c_int
         L.pa_oracle_traceback.argtypes = [ctypes.POINTER(OracleCfg), u8p, ctypes.c_uint64, u8p, ctypes.c_uint64,
                                           i64p, i64p, i64p, i64p, i64p, u8p, i64p]
         L.pa_oracle_traceback.restype = ctypes.c_int
@@ -140,20 +151,27 @@ def align_batch(cfg: OracleCfg, s1: np.ndarray, off1: np.ndarray, s2: np.ndarray
     return scores, e1, e2
 
 
-def simd_batch(cfg: OracleCfg, s1, off1, s2, off2, nthreads: int | None = None) -> np.ndarray:
-    """Inter-sequence int16-lane SIMD port (scores only) -- the timed CPU baseline."""
+def simd_batch(cfg: OracleCfg, s1, off1, s2, off2, nthreads: int | None = None, byte_lanes: bool = True,
+               counts: list | None = None) -> np.ndarray:
+    """Inter-sequence SIMD port (scores only) -- the timed CPU baseline.  Local alignment of
+    A/C/G/T pairs runs in 16 byte lanes (``byte_lanes``), the rest in 8 int16 or 4 int32 lanes;
+    ``counts`` (a list) receives the pairs finished at each width [byte, int16, int32]."""
     n = len(off1) - 1
     s1 = np.ascontiguousarray(s1, dtype=np.uint8)
     s2 = np.ascontiguousarray(s2, dtype=np.uint8)
     off1 = np.ascontiguousarray(off1, dtype=np.uint64)
     off2 = np.ascontiguousarray(off2, dtype=np.uint64)
     scores = np.empty(max(n, 1), np.int32)
+    cnt = np.zeros(3, np.uint64)
     nt = nthreads or os.cpu_count() or 1
-    rc = lib().pa_oracle_simd_batch(ctypes.byref(cfg), _ptr(s1, ctypes.c_uint8), _ptr(off1, ctypes.c_uint64),
-                                    _ptr(s2, ctypes.c_uint8), _ptr(off2, ctypes.c_uint64), n,
-                                    _ptr(scores, ctypes.c_int32), nt)
+    rc = lib().pa_oracle_simd_batch_lanes(ctypes.byref(cfg), _ptr(s1, ctypes.c_uint8), _ptr(off1, ctypes.c_uint64),
+                                          _ptr(s2, ctypes.c_uint8), _ptr(off2, ctypes.c_uint64), n,
+                                          _ptr(scores, ctypes.c_int32), nt, int(bool(byte_lanes)),
+                                          _ptr(cnt, ctypes.c_uint64))
     if rc:
-        raise RuntimeError(f"pa_oracle_simd_batch failed: {rc}")
+        raise RuntimeError(f"pa_oracle_simd_batch_lanes failed: {rc}")
+    if counts is not None:
+        counts[:] = [int(v) for v in cnt]
     return scores[:n]
 
 

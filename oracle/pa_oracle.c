@@ -25,13 +25,21 @@
  *     (the test/unit/affine scalar tests) by tests/test_oracle_golden.py.
  *
  *  2. pa_oracle_simd_batch -- a multi-threaded inter-sequence SIMD port of the
- *     reference's fixed-width SIMD path (cfg::score_model_unitary_simd,
- *     include/pairwise_aligner/configuration/score_model_unitary_simd.hpp:51-137):
- *     one alignment per vector lane (8 int16 lanes, or 4 int32 lanes for pairs
- *     whose scores could overflow int16), 16-byte GCC vector extensions (native
- *     on x86 SSE2 and Arm NEON), pthreads over batches.  Scores only, like the
- *     reference.  It is the timed CPU baseline where the reference itself can
- *     not be built.
+ *     reference's SIMD paths: one alignment per vector lane, 16-byte GCC vector
+ *     extensions (native on x86 SSE2 and Arm NEON), pthreads over batches.
+ *     Scores only, like the reference.  It is the timed CPU baseline where the
+ *     reference itself can not be built.  Lane widths:
+ *       - local alignment: 16 byte lanes per vector, as the reference's
+ *         saturated int8 model (cfg::score_model_unitary_simd_saturated,
+ *         configuration/score_model_unitary_simd_saturated.hpp:47-191), where
+ *         saturation at the low end implements the local clamp
+ *         (matrix/dp_vector_saturated_local.hpp:105-115).  Here the bytes hold
+ *         the true scores, floored at 0; a lane whose best score reaches the top
+ *         of the byte range is redone in int16 lanes (the reference rebases
+ *         instead, matrix/dp_matrix_column_saturated_local.hpp:65-84);
+ *       - otherwise 8 int16 lanes (cfg::score_model_unitary_simd<int16_t>,
+ *         configuration/score_model_unitary_simd.hpp:51-137), or 4 int32 lanes
+ *         for pairs whose scores could overflow int16.
  *
  * End-coordinate convention (the reference computes none: every tracker has
  * "TODO: optimal_coordinate()"): 1-based (i, j) = (end in sequence1, end in
@@ -366,6 +374,7 @@ int pa_oracle_align_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint6
  * earlier 32-byte build 17x slower per thread than its AVX2 build. */
 typedef int16_t v8s __attribute__((vector_size(16)));
 typedef int32_t v4i __attribute__((vector_size(16)));
+typedef uint8_t v16u __attribute__((vector_size(16)));
 
 typedef struct {
     const pa_oracle_cfg *cfg;
@@ -376,6 +385,7 @@ typedef struct {
     uint64_t next_batch;          /* shared work counter   */
     pthread_mutex_t lock;
     int32_t *scores;
+    uint8_t *redo;                /* byte lanes: pairs whose best score reached the byte limit */
     int rc;
 } simd_ctx;
 
@@ -453,6 +463,58 @@ static int FN(simd_ctx *x, const uint32_t *ids, int lanes, VT *qvec, VT *tvec, V
 PA_SIMD_BATCH(simd_batch16, v8s, int16_t, 8, INT16_MIN)
 PA_SIMD_BATCH(simd_batch32, v4i, int32_t, 4, INT32_MIN)
 
+/* Code of a byte in the byte-lane mode: A C G T -> 0..3; a pair qualifies only when all of
+ * its bytes are one of them, so equal codes are equal bytes, as the raw comparison of
+ * score_model_unitary::score (score_model/score_model_unitary.hpp:52-59) requires. */
+static inline int acgt_code(uint8_t b)
+{
+    return b == 'A' ? 0 : b == 'C' ? 1 : b == 'G' ? 2 : b == 'T' ? 3 : -1;
+}
+
+/* Local alignment in 16 unsigned-byte lanes.  A cell holds its true score (local scores are
+ * >= 0).  The subtractions are floored at 0: max(x, c) - c.  For H that is the local clamp of
+ * the diagonal term (dp_matrix_local.hpp:39-47); for the gap values it cannot change any H,
+ * because H is itself >= 0 (max(g, 0) - ext and g - ext lead to the same maxima with a value
+ * >= 0).  Additions of the match score cannot wrap while every value is <= 255 - match: the
+ * first cell that would exceed that bound is computed from smaller inputs without wrapping, so
+ * a lane whose best score stays <= 255 - match is exact and every other lane is redone.
+ * Padding codes (0xfe in sequence1, 0xff in sequence2) never match, so padded cells only
+ * lose score and never raise a lane's best. */
+/* The batch's DP (pa_oracle_bytes.cpp): sequence codes in, each lane's best score out. */
+void pa_oracle_byte_dp(const v16u *qvec, const v16u *tvec, v16u *hrow, v16u *vgap, uint64_t mmax, uint64_t nmax,
+                       uint8_t match, uint8_t mis, uint8_t goe, uint8_t ext, v16u *best_out);
+
+static int simd_batch8(simd_ctx *x, const uint32_t *ids, int lanes, v16u *qvec, v16u *tvec, v16u *hrow, v16u *vgap,
+                       size_t cap_n)
+{
+    enum { L = 16 };
+    const pa_oracle_cfg *c = x->cfg;
+    uint64_t mmax = 0, nmax = 0, ml[L], nl[L];
+    for (int l = 0; l < L; ++l) {
+        uint32_t k = ids[l < lanes ? l : 0];
+        ml[l] = x->off1[k + 1] - x->off1[k];
+        nl[l] = x->off2[k + 1] - x->off2[k];
+        if (ml[l] > mmax) mmax = ml[l];
+        if (nl[l] > nmax) nmax = nl[l];
+    }
+    if (nmax + 1 > cap_n || mmax + 1 > cap_n) return PA_ORACLE_ENOMEM;
+    for (int l = 0; l < L; ++l) {
+        uint32_t k = ids[l < lanes ? l : 0];
+        const uint8_t *a = x->s1 + x->off1[k], *b = x->s2 + x->off2[k];
+        for (uint64_t i = 0; i < mmax; ++i) qvec[i][l] = (uint8_t)(i < ml[l] ? acgt_code(a[i]) : 0xfe);
+        for (uint64_t j = 0; j < nmax; ++j) tvec[j][l] = (uint8_t)(j < nl[l] ? acgt_code(b[j]) : 0xff);
+    }
+    v16u best;
+    pa_oracle_byte_dp(qvec, tvec, hrow, vgap, mmax, nmax, (uint8_t)c->match, (uint8_t)(-c->mismatch),
+                      (uint8_t)(-(c->gap_open + c->gap_extension)), (uint8_t)(-c->gap_extension), &best);
+    const int limit = 255 - c->match;
+    for (int l = 0; l < lanes; ++l) {
+        if ((int)best[l] > limit) x->redo[ids[l]] = 1;
+        else x->scores[ids[l]] = (ml[l] == 0 || nl[l] == 0) ? INT32_MIN : (int32_t)best[l];
+    }
+    return PA_ORACLE_OK;
+}
+
 /* Workers pull batches of the lane count from a shared counter; each keeps its buffers. */
 #define PA_SIMD_WORKER(FN, BATCH, VT, L)                                                           \
 static void *FN(void *p)                                                                           \
@@ -496,6 +558,7 @@ static void *FN(void *p)                                                        
 
 PA_SIMD_WORKER(simd_worker16, simd_batch16, v8s, 8)
 PA_SIMD_WORKER(simd_worker32, simd_batch32, v4i, 4)
+PA_SIMD_WORKER(simd_worker8, simd_batch8, v16u, 16)
 
 static const uint64_t *g_sort_off1, *g_sort_off2;
 static int cmp_shape(const void *pa, const void *pb)
@@ -531,18 +594,61 @@ static int run_simd(simd_ctx *x, void *(*worker)(void *), int nthreads)
     return x->rc;
 }
 
-int pa_oracle_simd_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint64_t *off1,
-                         const uint8_t *s2, const uint64_t *off2, uint64_t n_pairs,
-                         int32_t *scores, int nthreads)
+/* The byte-lane mode applies to local alignment with scores that fit a byte; per pair, when
+ * both sequences are all A/C/G/T. */
+static int byte_lanes_apply(const pa_oracle_cfg *c)
+{
+    const int64_t goe = -(int64_t)c->gap_open - c->gap_extension, ext = -(int64_t)c->gap_extension;
+    return c->local && c->match > 0 && c->match <= 127 && c->mismatch <= 0 && c->mismatch >= -255 && goe >= 0 &&
+           goe <= 255 && ext >= 0 && ext <= 255;
+}
+
+static int pair_is_acgt(const uint8_t *s1, uint64_t m, const uint8_t *s2, uint64_t n)
+{
+    for (uint64_t i = 0; i < m; ++i) if (acgt_code(s1[i]) < 0) return 0;
+    for (uint64_t j = 0; j < n; ++j) if (acgt_code(s2[j]) < 0) return 0;
+    return 1;
+}
+
+int pa_oracle_simd_batch_lanes(const pa_oracle_cfg *c, const uint8_t *s1, const uint64_t *off1,
+                               const uint8_t *s2, const uint64_t *off2, uint64_t n_pairs,
+                               int32_t *scores, int nthreads, int byte_lanes, uint64_t counts[3])
 {
     if (!c || !scores || (n_pairs && (!off1 || !off2))) return PA_ORACLE_EINVAL;
     if (c->local == 0 && (c->last_column_free || c->last_row_free)) return PA_ORACLE_EINVAL;
     if (c->dim) return PA_ORACLE_EINVAL;                /* the SIMD port scores unitary only */
+    if (counts) counts[0] = counts[1] = counts[2] = 0;
+    if (nthreads < 1) nthreads = 1;
+    uint8_t *redo = NULL;
+    const int use8 = byte_lanes && byte_lanes_apply(c) && n_pairs;
+    if (use8) {
+        /* byte lanes first; the pairs they cannot finish fall through to the wider lanes */
+        uint32_t *order8 = (uint32_t *)malloc(sizeof(uint32_t) * n_pairs);
+        redo = (uint8_t *)calloc(n_pairs, 1);
+        if (!order8 || !redo) { free(order8); free(redo); return PA_ORACLE_ENOMEM; }
+        uint64_t n8 = 0;
+        for (uint64_t k = 0; k < n_pairs; ++k) {
+            const uint64_t m = off1[k + 1] - off1[k], n = off2[k + 1] - off2[k];
+            if (pair_is_acgt(s1 + off1[k], m, s2 + off2[k], n)) order8[n8++] = (uint32_t)k;
+            else redo[k] = 1;
+        }
+        g_sort_off1 = off1; g_sort_off2 = off2;
+        qsort(order8, n8, sizeof(uint32_t), cmp_shape);
+        simd_ctx x;
+        memset(&x, 0, sizeof(x));
+        x.cfg = c; x.s1 = s1; x.off1 = off1; x.s2 = s2; x.off2 = off2; x.scores = scores; x.redo = redo;
+        x.order = order8; x.n_pairs = n8;
+        int rc = n8 ? run_simd(&x, simd_worker8, nthreads) : PA_ORACLE_OK;
+        free(order8);
+        if (rc) { free(redo); return rc; }
+        if (counts) for (uint64_t k = 0; k < n_pairs; ++k) counts[0] += !redo[k];
+    }
     uint32_t *order = (uint32_t *)malloc(sizeof(uint32_t) * (n_pairs ? n_pairs : 1) * 2);
-    if (!order) return PA_ORACLE_ENOMEM;
+    if (!order) { free(redo); return PA_ORACLE_ENOMEM; }
     uint32_t *order32 = order + (n_pairs ? n_pairs : 1);
     uint64_t n16 = 0, n32 = 0;
     for (uint64_t k = 0; k < n_pairs; ++k) {
+        if (redo && !redo[k]) continue;               /* finished in byte lanes */
         uint64_t m = off1[k + 1] - off1[k], n = off2[k + 1] - off2[k];
         const int64_t bound = lane_bound(c, m, n);
         if (bound < 32000) order[n16++] = (uint32_t)k;
@@ -550,14 +656,15 @@ int pa_oracle_simd_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint64
         else {                                    /* too wide for int32 lanes: scalar int64 */
             int64_t sc, e1, e2;
             int rc = pa_oracle_align(c, s1 + off1[k], m, s2 + off2[k], n, &sc, &e1, &e2);
-            if (rc) { free(order); return rc; }
+            if (rc) { free(order); free(redo); return rc; }
             scores[k] = (int32_t)sc;
         }
     }
+    free(redo);
+    if (counts) { counts[1] = n16; counts[2] = n32; }
     g_sort_off1 = off1; g_sort_off2 = off2;
     qsort(order, n16, sizeof(uint32_t), cmp_shape);
     qsort(order32, n32, sizeof(uint32_t), cmp_shape);
-    if (nthreads < 1) nthreads = 1;
     simd_ctx x;
     memset(&x, 0, sizeof(x));
     x.cfg = c; x.s1 = s1; x.off1 = off1; x.s2 = s2; x.off2 = off2; x.scores = scores;
@@ -569,4 +676,12 @@ int pa_oracle_simd_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint64
     }
     free(order);
     return rc;
+}
+
+/* All lane widths the port has (byte lanes where they apply). */
+int pa_oracle_simd_batch(const pa_oracle_cfg *c, const uint8_t *s1, const uint64_t *off1,
+                         const uint8_t *s2, const uint64_t *off2, uint64_t n_pairs,
+                         int32_t *scores, int nthreads)
+{
+    return pa_oracle_simd_batch_lanes(c, s1, off1, s2, off2, n_pairs, scores, nthreads, 1, NULL);
 }

@@ -156,3 +156,50 @@ def test_simd_port_matches_scalar_on_random_configs(oracle):
         got = oracle.simd_batch(cfg, q, qo, t, to, nthreads=4)
         want, _, _ = oracle.align_batch(cfg, q, qo, t, to, nthreads=4)
         assert list(got) == list(want), (trial, match, mismatch, go, ge, local, fc, fr)
+
+
+@pytest.mark.parametrize("byte_lanes", [True, False])
+def test_simd_port_lane_widths_match_scalar(oracle, simd_cases, byte_lanes):
+    """Local cases through the byte lanes (the reference's saturated int8 width) and through
+    int16 lanes only: both equal the scalar restatement; the byte lanes really run."""
+    from pairwise_aligner_gb300.aligner import pack
+    ran8 = 0
+    for c in simd_cases:
+        if c["method"] != "local":
+            continue
+        cfg = oracle_cfg_of(oracle, c)
+        s1, o1 = pack(c["seqs1"])
+        s2, o2 = pack(c["seqs2"])
+        counts = [0, 0, 0]
+        got = oracle.simd_batch(cfg, s1, o1, s2, o2, nthreads=2, byte_lanes=byte_lanes, counts=counts)
+        assert list(got) == c["oracle_scores"], c["name"]
+        assert sum(counts) <= len(got) and (byte_lanes or counts[0] == 0)
+        ran8 += counts[0]
+    assert (ran8 > 0) == byte_lanes
+
+
+def test_byte_lanes_redo_saturated_pairs_exactly(oracle):
+    """Pairs whose local score passes the byte range (long identical runs, large match scores)
+    are redone in wider lanes; scores still equal the scalar oracle."""
+    from pairwise_aligner_gb300.aligner import pack
+    rng = np.random.default_rng(41)
+    acgt = np.frombuffer(b"ACGT", dtype=np.uint8)
+    for match in (1, 3, 100):
+        cfg = oracle.make_cfg(match, -4, -6, -1, local=True)
+        s1, s2 = [], []
+        for k in range(48):
+            n = int(rng.integers(0, 700))
+            a = acgt[rng.integers(0, 4, n)]
+            b = a.copy() if k % 3 == 0 else acgt[rng.integers(0, 4, int(rng.integers(0, 700)))]
+            s1.append(a.tobytes())
+            s2.append(b.tobytes())
+        s1.append(b"ACGTN")                           # a non-ACGT byte: wider lanes
+        s2.append(b"ACGTN")
+        q, qo = pack(s1)
+        t, to = pack(s2)
+        counts = [0, 0, 0]
+        got = oracle.simd_batch(cfg, q, qo, t, to, nthreads=3, counts=counts)
+        want, _, _ = oracle.align_batch(cfg, q, qo, t, to, nthreads=3)
+        assert list(got) == list(want), match
+        assert counts[1] + counts[2] > 0, counts      # saturated or non-ACGT pairs went wider
+        assert counts[0] > 0 or match == 100, counts   # with match 100 nearly every lane saturates
