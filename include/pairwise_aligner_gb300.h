@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define PA_ABI_VERSION 1
+#define PA_ABI_VERSION 2
 
 typedef enum pa_status {
     PA_OK = 0,
@@ -111,7 +111,7 @@ typedef struct pa_options {
     int32_t blocks_per_sm;      /* persistent grid occupancy: 0 auto                       */
     int32_t use_graphs;         /* 0 auto(on), 1 on, -1 off                                */
     int32_t autotune;           /* 0 off, 1 on first use                                   */
-    int32_t kernel_variant;     /* inner-loop form: -1 auto (per-method tuning), else 0..8 (pa_tuning) */
+    int32_t kernel_variant;     /* inner-loop form: -1 auto (tuning table), else 0..10 (pa_tuning) */
     int32_t reserved[2];
 } pa_options;
 
@@ -315,22 +315,41 @@ pa_status pa_align_batch_banded(pa_ctx *ctx, const pa_config *config,
 
 /* Kernel choices of a context.  Replaces nothing in the reference (its tile
  * shapes are compile-time lane widths, simd/simd_base.hpp:28-57).
- * variant: inner-loop form of the DP (0 three-operand max, 1 short chain,
- * 2 three-operand with at most 85 registers, 3 branch-free top input with L1
- * prefetch, 4 as 3 with a two-op vertical-gap chain, 5 / 6 as 3 / 4 with one
- * prefetch per 8 columns, 7 / 8 as 3 / 4 without the score-table prefetch); group_threads: lanes
- * per pair group (1..32, power of two).  Index 0 = local, 1 = global. */
+ * variant: inner-loop form of the DP: 0..8 the general kernel (0 three-operand max,
+ * 1 short chain, 2 three-operand with at most 85 registers, 3 branch-free top input with
+ * L1 prefetch, 4 as 3 with a two-op vertical-gap chain, 5 / 6 as 3 / 4 with one prefetch
+ * per 8 columns, 7 / 8 as 3 / 4 without the score-table prefetch), 9 / 10 the short-pair
+ * s16x2 kernel with 16 / 32 rows of sequence2 per thread (unitary DNA scores; other
+ * classes take the general kernel's default); group_threads: lanes per pair group (1..32,
+ * power of two; 0: the built-in rule, which picks it from the batch size).  Index 0 =
+ * local, 1 = global.
+ * The s16x2 class also has a table of tuned entries, one per method, batch-size class
+ * and pair-size class: size class s = 0..3 when n_pairs < 2^(12 + 2s), else 4; pair-size
+ * class h = 0..2 when the mean m*n per pair < 2^(14 + 2h), else 3.  An entry with
+ * group_threads 0 falls back to variant_s16 / group_threads_s16; when that group size is
+ * 0 too and variant_s16 is a short-pair variant, the rule also picks its rows per thread
+ * (32 for groups of up to 8 lanes, else 16). */
+#define PA_TUNE_SIZES 5
+#define PA_TUNE_SHAPES 4
+typedef struct pa_tune_entry {
+    int16_t variant;            /* 0..10                                                   */
+    int16_t group_threads;      /* 1..32, power of two; 0: not tuned                       */
+    float dp_ms;                /* pa_autotune: device time of the chosen candidate        */
+} pa_tune_entry;
+
 typedef struct pa_tuning {
     int32_t variant_s16[2];
     int32_t variant_s32[2];
     int32_t group_threads_s16[2];
     int32_t group_threads_s32[2];
     double best_ms[2];          /* pa_autotune: device time of the chosen candidate        */
+    pa_tune_entry s16[2][PA_TUNE_SIZES][PA_TUNE_SHAPES];
 } pa_tuning;
 
-/* Time every (variant, group_threads) candidate on this batch (host buffers,
- * as pa_align_batch) and keep the fastest for the config's method on this
- * context; the choice is also written to *out (may be NULL). */
+/* Time every (variant, group_threads) candidate of the s16x2 class on this batch (host
+ * buffers, as pa_align_batch) and keep the fastest in the table entry of the batch's
+ * method, size class and pair-size class; the whole tuning is also written to *out (may be
+ * NULL). */
 pa_status pa_autotune(pa_ctx *ctx, const pa_config *config,
                       const uint8_t *seq1, const uint64_t *off1,
                       const uint8_t *seq2, const uint64_t *off2,

@@ -103,6 +103,17 @@ class PaBandOptions(ctypes.Structure):
     ]
 
 
+TUNE_SIZES, TUNE_SHAPES = 5, 4          # PA_TUNE_SIZES, PA_TUNE_SHAPES
+
+
+class PaTuneEntry(ctypes.Structure):
+    _fields_ = [
+        ("variant", ctypes.c_int16),
+        ("group_threads", ctypes.c_int16),
+        ("dp_ms", ctypes.c_float),
+    ]
+
+
 class PaTuning(ctypes.Structure):
     _fields_ = [
         ("variant_s16", ctypes.c_int32 * 2),
@@ -110,7 +121,30 @@ class PaTuning(ctypes.Structure):
         ("group_threads_s16", ctypes.c_int32 * 2),
         ("group_threads_s32", ctypes.c_int32 * 2),
         ("best_ms", ctypes.c_double * 2),
+        ("s16", PaTuneEntry * TUNE_SHAPES * TUNE_SIZES * 2),
     ]
+
+
+def tuning_to_dict(t: PaTuning) -> dict:
+    """A PaTuning as plain lists (the s16 table as [method][size class][pair-size class] dicts)."""
+    out = {name: list(getattr(t, name)) for name in ("variant_s16", "variant_s32", "group_threads_s16",
+                                                      "group_threads_s32", "best_ms")}
+    out["s16"] = [[[{"variant": e.variant, "group_threads": e.group_threads, "dp_ms": e.dp_ms} for e in row]
+                   for row in m] for m in t.s16]
+    return out
+
+
+def tuning_from_dict(d: dict) -> PaTuning:
+    t = PaTuning()
+    for name in ("variant_s16", "variant_s32", "group_threads_s16", "group_threads_s32", "best_ms"):
+        getattr(t, name)[:] = d[name]
+    for mi, m in enumerate(d.get("s16", [])):
+        for a, row in enumerate(m):
+            for b, e in enumerate(row):
+                t.s16[mi][a][b].variant = int(e["variant"])
+                t.s16[mi][a][b].group_threads = int(e["group_threads"])
+                t.s16[mi][a][b].dp_ms = float(e["dp_ms"])
+    return t
 
 
 class PaRoofline(ctypes.Structure):

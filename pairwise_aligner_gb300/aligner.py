@@ -122,18 +122,18 @@ class Context:
 
     # -- kernel choices -------------------------------------------------------
     def tuning(self) -> dict:
+        """Kernel choices: per-method defaults and the s16x2 table [method][size class][pair-size class]."""
         t = _lib.PaTuning()
         _lib.check(self.lib.pa_get_tuning(self.ptr, ctypes.byref(t)), self.ptr)
-        return {name: list(getattr(t, name)) for name, _ in _lib.PaTuning._fields_}
+        return _lib.tuning_to_dict(t)
 
     def set_tuning(self, tuning: dict):
-        t = _lib.PaTuning()
-        for name, _ in _lib.PaTuning._fields_:
-            getattr(t, name)[:] = tuning[name]
+        t = _lib.tuning_from_dict(tuning)
         _lib.check(self.lib.pa_set_tuning(self.ptr, ctypes.byref(t)), self.ptr)
 
     def autotune(self, c_config, seq1, off1, seq2, off2) -> dict:
-        """Time the kernel candidates on this batch and keep the fastest for its method."""
+        """Time the kernel candidates on this batch and keep the fastest in the table entry of
+        the batch's method, batch-size class and pair-size class."""
         seq1 = np.ascontiguousarray(seq1, dtype=np.uint8)
         seq2 = np.ascontiguousarray(seq2, dtype=np.uint8)
         off1 = np.ascontiguousarray(off1, dtype=np.uint64)
@@ -142,7 +142,7 @@ class Context:
         _lib.check(self.lib.pa_autotune(self.ptr, ctypes.byref(c_config), seq1.ctypes.data, off1.ctypes.data,
                                         seq2.ctypes.data, off2.ctypes.data, len(off1) - 1, ctypes.byref(t)),
                    self.ptr)
-        return {name: list(getattr(t, name)) for name, _ in _lib.PaTuning._fields_}
+        return _lib.tuning_to_dict(t)
 
     def save_tuning(self, path: str):
         import json

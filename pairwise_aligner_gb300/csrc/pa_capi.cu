@@ -35,6 +35,7 @@ constexpr int64_t kDefaultRingM = 65536;   // device entry points: CTA mode up t
 constexpr int kDefaultG = 8;       // threads per group
 constexpr int kShortVariant = 9;   // variants 9, 10: dp_short (s16x2 unitary short pairs), 16 / 32 rows per thread
 constexpr int kVariants = kShortVariant + kShortFormCount;   // 0..8: dp_kernel (pa_kern_v*.cu)
+constexpr int kDefaultShortVariant = kShortVariant;          // with the rule below: 16 or 32 rows per thread
 
 struct DevBuf {
     void *p = nullptr;
@@ -86,7 +87,7 @@ struct pa_ctx {
     DevBuf in_seq1, in_off1, in_seq2, in_off2, in_out;   // staging for the host-buffer entry points
     int G[3] = {kDefaultG, kDefaultG, kDefaultG};
     int variant[3] = {0, 0, 0};
-    pa_tuning tuning{};           // per method (0 local, 1 global); applied to G/variant per call
+    pa_tuning tuning{};           // per method (0 local, 1 global) and s16 table; applied per call
     bool fixed_G = false, fixed_variant = false;
     int grid[3] = {0, 0, 0};
     std::map<GraphKey, GraphEntry> graphs;
@@ -557,17 +558,52 @@ pa_status prepare_buffers(pa_ctx *c, uint64_t n_pairs, uint64_t b1)
     return PA_OK;
 }
 
-void apply_tuning(pa_ctx *c, const pa_config *cfg)
+// Buckets of the s16x2 tuning table (pa_tuning::s16): batch-size class and pair-size class.
+int tune_size_class(uint64_t n_pairs)
+{
+    for (int s = 0; s < PA_TUNE_SIZES - 1; ++s)
+        if (n_pairs < (1ull << (12 + 2 * s))) return s;
+    return PA_TUNE_SIZES - 1;
+}
+
+int tune_shape_class(uint64_t n_pairs, uint64_t b1, uint64_t b2)
+{
+    const double mean = n_pairs ? ((double)b1 / (double)n_pairs) * ((double)b2 / (double)n_pairs) : 0.0;
+    for (int h = 0; h < PA_TUNE_SHAPES - 1; ++h)
+        if (mean < (double)(1ull << (14 + 2 * h))) return h;
+    return PA_TUNE_SHAPES - 1;
+}
+
+// The built-in group size: the smallest group (fewest fill and drain steps per pass) that
+// still gives every resident warp about eight work units, so the persistent queue's tail
+// stays short.  A warp unit holds 32 / G groups of `lanes` pairs.
+int rule_group_threads(const pa_ctx *c, uint64_t n_pairs, int lanes)
+{
+    const double warps = (double)c->sm_count * (2 * kBlock / 32);
+    for (int g = 4; g < 32; g *= 2)
+        if ((double)n_pairs * g / (32.0 * lanes) >= 8.0 * warps) return g;
+    return 32;
+}
+
+void apply_tuning(pa_ctx *c, const pa_config *cfg, uint64_t n_pairs, uint64_t b1, uint64_t b2)
 {
     if (!cfg) return;
     const int mi = (cfg->method & ~PA_SCORE_MATRIX) == PA_METHOD_LOCAL ? 0 : 1;
+    const pa_tune_entry &e = c->tuning.s16[mi][tune_size_class(n_pairs)][tune_shape_class(n_pairs, b1, b2)];
     if (!c->fixed_variant) {
-        c->variant[K_S16] = c->tuning.variant_s16[mi];
+        c->variant[K_S16] = e.group_threads ? e.variant : c->tuning.variant_s16[mi];
         c->variant[K_S32] = c->variant[K_GEN] = c->tuning.variant_s32[mi];
     }
     if (!c->fixed_G) {
-        c->G[K_S16] = c->tuning.group_threads_s16[mi];
-        c->G[K_S32] = c->G[K_GEN] = c->tuning.group_threads_s32[mi];
+        int g16 = e.group_threads ? e.group_threads : c->tuning.group_threads_s16[mi];
+        int g32 = c->tuning.group_threads_s32[mi];
+        c->G[K_S16] = g16 ? g16 : rule_group_threads(c, n_pairs, 2);
+        c->G[K_S32] = c->G[K_GEN] = g32 ? g32 : rule_group_threads(c, n_pairs, 1);
+        // untuned short-pair kernel: 32 rows per thread where groups are small (large batches;
+        // half the column steps of 16 rows), 16 where they are large (few pairs: 32 rows would
+        // make passes of 512-1,024 rows, mostly padding for short pairs)
+        if (!e.group_threads && !g16 && !c->fixed_variant && c->tuning.variant_s16[mi] >= kShortVariant)
+            c->variant[K_S16] = c->G[K_S16] <= 8 ? kShortVariant + 1 : kShortVariant;
     }
 }
 
@@ -613,7 +649,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
                    const uint8_t *s2, const uint64_t *o2, uint64_t b2, uint64_t n_pairs, pa_result *out,
                    const int32_t *h_bands, pa_stats *stats)
 {
-    apply_tuning(c, cfg);
+    apply_tuning(c, cfg, n_pairs, b1, b2);
     pa_status s = n_pairs ? ensure_ring(c, c->want_ring_m) : PA_OK;
     if (s) return s;
     DpParams P;
@@ -949,7 +985,7 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
                      pa_stats *stats, bool sync_for_stats)
 {
     if (cfg && cfg->band_mode) return run_band(c, cfg, s1, o1, b1, s2, o2, b2, n_pairs, out, nullptr, stats);
-    apply_tuning(c, cfg);
+    apply_tuning(c, cfg, n_pairs, b1, b2);
     pa_status s = n_pairs ? ensure_ring(c, c->want_ring_m) : PA_OK;
     if (s) return s;
     DpParams P;
@@ -1112,7 +1148,10 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
     }
     // defaults measured on GB300 (262,144 pairs of 64..512 bp): local s16x2 is fastest with
     // variant 7, global with variant 4; 8 lanes per group
-    c->tuning = pa_tuning{{7, 4}, {0, 4}, {8, 8}, {8, 8}, {0.0, 0.0}};
+    c->tuning = pa_tuning{};
+    c->tuning.variant_s16[0] = c->tuning.variant_s16[1] = kDefaultShortVariant;
+    c->tuning.variant_s32[0] = 0;
+    c->tuning.variant_s32[1] = 4;                 // group sizes 0: the built-in rule
     if (c->opt.group_threads) {
         int g = c->opt.group_threads;
         if (g < 1 || g > 32 || (g & (g - 1))) { pa_destroy(c); return PA_ERR_INVALID_ARGUMENT; }
@@ -1765,7 +1804,7 @@ pa_status pa_get_tuning(const pa_ctx *ctx, pa_tuning *out)
     return PA_OK;
 }
 
-static bool valid_G(int g) { return g >= 1 && g <= 32 && (g & (g - 1)) == 0; }
+static bool valid_G(int g) { return g == 0 || (g >= 1 && g <= 32 && (g & (g - 1)) == 0); }
 static bool valid_variant(int v) { return v >= 0 && v < kVariants; }
 
 pa_status pa_set_tuning(pa_ctx *ctx, const pa_tuning *t)
@@ -1774,7 +1813,15 @@ pa_status pa_set_tuning(pa_ctx *ctx, const pa_tuning *t)
     for (int m = 0; m < 2; ++m)
         if (!valid_variant(t->variant_s16[m]) || !valid_variant(t->variant_s32[m]) || !valid_G(t->group_threads_s16[m]) ||
             !valid_G(t->group_threads_s32[m]))
-            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "tuning: variant must be 0..10 and group_threads 1..32, power of two");
+            return fail(ctx, PA_ERR_INVALID_ARGUMENT,
+                        "tuning: variant must be 0..10 and group_threads 0 or 1..32, power of two");
+    for (int m = 0; m < 2; ++m)
+        for (int a = 0; a < PA_TUNE_SIZES; ++a)
+            for (int b = 0; b < PA_TUNE_SHAPES; ++b) {
+                const pa_tune_entry &e = t->s16[m][a][b];
+                if (!valid_variant(e.variant) || !valid_G(e.group_threads))
+                    return fail(ctx, PA_ERR_INVALID_ARGUMENT, "tuning table: variant 0..10, group_threads 0..32");
+            }
     ctx->tuning = *t;
     ctx->fixed_G = ctx->fixed_variant = false;
     return PA_OK;
@@ -1784,33 +1831,40 @@ pa_status pa_autotune(pa_ctx *ctx, const pa_config *config, const uint8_t *seq1,
                       const uint8_t *seq2, const uint64_t *off2, uint64_t n_pairs, pa_tuning *out)
 {
     if (!ctx || !config) return PA_ERR_INVALID_ARGUMENT;
+    if (n_pairs && (!off1 || !off2)) return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null offsets");
     const int mi = (config->method & ~PA_SCORE_MATRIX) == PA_METHOD_LOCAL ? 0 : 1;
-    const pa_tuning saved = ctx->tuning;
+    const uint64_t b1 = n_pairs ? off1[n_pairs] - off1[0] : 0, b2 = n_pairs ? off2[n_pairs] - off2[0] : 0;
+    pa_tune_entry &slot = ctx->tuning.s16[mi][tune_size_class(n_pairs)][tune_shape_class(n_pairs, b1, b2)];
+    const pa_tune_entry saved = slot;
     const bool fg = ctx->fixed_G, fv = ctx->fixed_variant;
     ctx->fixed_G = ctx->fixed_variant = false;
     std::vector<pa_result> res(std::max<uint64_t>(n_pairs, 1));
+    // the short-pair kernel with 16 and 32 rows per thread at every group size it has, and the
+    // general kernel down to one pair per lane (two per thread in s16x2 halves)
+    struct Cand { int v, g; };
+    std::vector<Cand> cands;
+    for (int v = kShortVariant; v < kVariants; ++v)
+        for (int g : {4, 8, 16, 32}) cands.push_back({v, g});
+    for (int g : {1, 2, 4, 8, 16, 32}) cands.push_back({mi == 0 ? 7 : 4, g});
     double best = 1e300;
-    pa_tuning choice = saved;
-    static const int kCandidates[] = {0, 1, 3, 4, 5, 6, 7, 8};
-    static const int kGroups[] = {4, 8, 16};
-    for (int v : kCandidates)
-        for (int g : kGroups) {
-            pa_tuning t = saved;
-            t.variant_s16[mi] = t.variant_s32[mi] = v;
-            t.group_threads_s16[mi] = t.group_threads_s32[mi] = g;
-            ctx->tuning = t;
-            double ms = 1e300;
-            for (int rep = 0; rep < 3; ++rep) {                 // first run captures the graph
-                pa_stats st;
-                pa_status s = pa_align_batch(ctx, config, seq1, off1, seq2, off2, n_pairs, res.data(), &st);
-                if (s) { ctx->tuning = saved; ctx->fixed_G = fg; ctx->fixed_variant = fv; return s; }
-                if (rep > 0) ms = std::min(ms, st.dp_ms);
-            }
-            if (ms < best) { best = ms; choice = t; }
+    pa_tune_entry choice = saved;
+    for (const Cand &cd : cands) {
+        slot = pa_tune_entry{(int16_t)cd.v, (int16_t)cd.g, 0.f};
+        double ms = 1e300;
+        for (int rep = 0; rep < 3; ++rep) {                 // first run captures the graph
+            pa_stats st;
+            pa_status s = pa_align_batch(ctx, config, seq1, off1, seq2, off2, n_pairs, res.data(), &st);
+            if (s) { slot = saved; ctx->fixed_G = fg; ctx->fixed_variant = fv; return s; }
+            if (rep > 0) ms = std::min(ms, st.dp_ms);
         }
-    choice.best_ms[mi] = best;
-    ctx->tuning = choice;
-    if (out) *out = choice;
+        if (ms < best) { best = ms; choice = slot; choice.dp_ms = (float)ms; }
+    }
+    slot = choice;
+    ctx->tuning.best_ms[mi] = best;
+    ctx->fixed_G = fg;
+    ctx->fixed_variant = fv;
+    drop_graphs(ctx);                                       // the candidates' captures
+    if (out) *out = ctx->tuning;
     return PA_OK;
 }
 

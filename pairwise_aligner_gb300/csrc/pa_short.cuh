@@ -11,9 +11,9 @@
 //    top vertical gap}.  The group writes the slots of its unit once (tables from the
 //    sequence1 bytes, the top border of the first pass); the last thread writes the
 //    pass's bottom row back into the .h/.e halves for the next pass;
-//  * the group's shuffle is a rotation: thread t receives thread t-1's bottom H, gap and
-//    score tables, and thread 0 receives thread G-1's registers, into which thread G-1
-//    loads the slot of thread 0's next column (one 16-byte load per column, no select);
+//  * thread 0 reads one slot per column with a single vector load, one column ahead, and
+//    the score tables travel down the group with the H and gap values by shuffle, so no
+//    other thread loads anything per column (thread 0 selects the slot's values);
 //  * the rows are written so that the diagonal term of row k + 1 is formed before row k's
 //    new H replaces the old one (no register copies between column steps);
 //  * the unit's description, the per-thread candidates and the column of the last local
@@ -83,20 +83,16 @@ __device__ __forceinline__ void short_pass(const DpLaunch &L, const DpParams &P,
     }
     uint32_t prevH = stored(border(P, P.first_row_free, j0));
     const bool writer = t == G - 1 && p + 1 < u.passes;
-    const bool feeder = t == G - 1;               // loads thread 0's next slot
-    const int src = (t + G - 1) & (G - 1);        // rotation: thread 0 hears thread G - 1
+    const bool t0 = t == 0;
     const int32_t ms = u.ms;
     Slot *const slot = u.slot;
     const int32_t um[2] = {u.m[0], u.m[1]}, un[2] = {u.n[0], u.n[1]};
     const bool has_b = u.has_b != 0;
 
-    // the registers a thread hands on: bottom H and gap of its strip and the column's tables;
-    // thread G - 1's are the slot of thread 0's next column instead
+    // the registers a thread hands on: bottom H and gap of its strip and the column's tables
     uint32_t sH = 0, sE = 0, sA = 0, sB = 0;
-    if (feeder) {
-        const uint4 v = *reinterpret_cast<const uint4 *>(slot + 1);
-        sA = v.x; sB = v.y; sH = v.z; sE = v.w;
-    }
+    uint4 nx = make_uint4(0u, 0u, 0u, 0u);        // thread 0: the slot of its next column
+    if (t0) nx = *reinterpret_cast<const uint4 *>(slot + 1);
     uint32_t best = V::splat(KC::Kt);
     // global modes: where rows n[0], n[1] live
     int32_t own_k[2] = {0, 0};
@@ -113,11 +109,16 @@ __device__ __forceinline__ void short_pass(const DpLaunch &L, const DpParams &P,
     // step s of the pass: thread t computes column i = s - t + 1 when 1 <= i <= ms
     auto step = [&](int32_t s, bool active) {
         const int32_t i = s - t + 1;
-        const uint32_t upH = __shfl_sync(gmask, sH, src, G);
-        uint32_t Ed = __shfl_sync(gmask, sE, src, G);
-        const uint32_t ta = __shfl_sync(gmask, sA, src, G);
-        const uint32_t tb = __shfl_sync(gmask, sB, src, G);
+        const uint32_t xH = __shfl_up_sync(gmask, sH, 1, G);
+        const uint32_t xE = __shfl_up_sync(gmask, sE, 1, G);
+        const uint32_t xA = __shfl_up_sync(gmask, sA, 1, G);
+        const uint32_t xB = __shfl_up_sync(gmask, sB, 1, G);
         if (active) {
+            const uint32_t upH = t0 ? nx.z : xH;
+            uint32_t Ed = t0 ? nx.w : xE;
+            const uint32_t ta = t0 ? nx.x : xA;
+            const uint32_t tb = t0 ? nx.y : xB;
+            if (t0 && i < ms) nx = *reinterpret_cast<const uint4 *>(slot + i + 1);
             uint32_t tt = V::addmax(prevH, prmt(ta, tb, Sel[0]), Fr[0]);
 #pragma unroll
             for (int k = 0; k < RA; ++k) {
@@ -180,11 +181,6 @@ __device__ __forceinline__ void short_pass(const DpLaunch &L, const DpParams &P,
                     }
                 }
             }
-        }
-        // thread G - 1 hands thread 0 the slot of column s + 2 at the next step
-        if (feeder && s + 2 <= ms) {
-            const uint4 v = *reinterpret_cast<const uint4 *>(slot + s + 2);
-            sA = v.x; sB = v.y; sH = v.z; sE = v.w;
         }
     };
     // fill: thread t starts at step t; steady: every thread active; drain

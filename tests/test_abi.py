@@ -60,7 +60,7 @@ def test_python_binding_argument_counts_match_the_header(built_lib):
 def test_status_strings_and_version(built_lib):
     from pairwise_aligner_gb300 import _lib
     lib = _lib.load()
-    assert lib.pa_abi_version() == 1
+    assert lib.pa_abi_version() == 2
     assert lib.pa_status_string(0) == b"ok"
     for code in range(1, 9):
         assert lib.pa_status_string(code) not in (b"", b"unknown status")

@@ -227,23 +227,44 @@ def test_invalid_arguments(pa):
         ok.compute_arrays(*pa.pack(["A", "C"]), *pa.pack(["A"]))
 
 
-def test_autotune_keeps_results_exact(pa, oracle, tmp_path):
+def test_autotune_fills_the_batch_bucket_and_stays_exact(pa, oracle, tmp_path):
+    """pa_autotune times the candidates on this batch and keeps the winner in the table entry
+    of its method, batch-size class (2,048 pairs: class 0) and pair-size class (mean m*n of
+    about 82,000: class 2); the other entries stay untuned; the choice survives a save/load."""
     from pairwise_aligner_gb300 import workloads as W
     d = W.config2(seed=17, n_pairs=2048)
     al = _aligner_for(pa, d)
     ctx = al.context
     before = ctx.tuning()
     t = ctx.autotune(al.c_config(), d["seq1"], d["off1"], d["seq2"], d["off2"])
-    assert t["variant_s16"][0] in (0, 1, 3, 4, 5, 6, 7, 8) and t["group_threads_s16"][0] in (4, 8, 16)
-    assert t["best_ms"][0] > 0
-    assert t["variant_s16"][1] == before["variant_s16"][1]          # the other method is untouched
+    e = t["s16"][0][0][2]
+    assert 0 <= e["variant"] <= 10 and e["group_threads"] in (1, 2, 4, 8, 16, 32) and e["dp_ms"] > 0
+    for mi in range(2):
+        for a in range(5):
+            for b in range(4):
+                if (mi, a, b) != (0, 0, 2):
+                    assert t["s16"][mi][a][b] == before["s16"][mi][a][b]
     res = al.compute_arrays(d["seq1"], d["off1"], d["seq2"], d["off2"])
     _check(oracle, d, res)
     path = str(tmp_path / "tuning.json")
     ctx.save_tuning(path)
     fresh = pa.Context(0)
     fresh.load_tuning(path)
-    assert fresh.tuning()["variant_s16"] == t["variant_s16"]
+    assert fresh.tuning()["s16"] == t["s16"]
+
+
+@pytest.mark.parametrize("local", [True, False])
+def test_every_autotune_candidate_is_exact(pa, oracle, local):
+    """Each (kernel variant, group size) pa_autotune can choose: the short-pair kernel with 16
+    and 32 rows per thread at G = 4..32, and the general kernel down to G = 1 (one pair per
+    lane, two per thread in s16x2 halves)."""
+    from pairwise_aligner_gb300 import workloads as W
+    d = W.config2(seed=19, n_pairs=1024) if local else W.config4(seed=19, n_pairs=512)
+    cands = [(v, g) for v in (9, 10) for g in (4, 8, 16, 32)] + [(7 if local else 4, g) for g in (1, 2, 4, 8, 16, 32)]
+    for v, g in cands:
+        res = _aligner_for(pa, d, group_threads=g, kernel_variant=v).compute_arrays(
+            d["seq1"], d["off1"], d["seq2"], d["off2"])
+        _check(oracle, d, res)
 
 
 def test_config5_stratified_sample(pa, oracle):
