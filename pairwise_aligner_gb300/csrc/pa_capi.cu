@@ -694,19 +694,31 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, st));
     PA_CUDA(c, cudaMemsetAsync(c->band_ctr.p, 0, 256, st));
     if ((s = enqueue_prep(c, P, C, s1, o1, b1, s2, o2, b2, out, np))) return s;
+    uint32_t ranges[16], counts[16];
     {
         // the classifier checked the offsets; a batch with inconsistent ones is not aligned (and
         // the band features, which read the sequences, must not run on it)
         unsigned long long bad = 0;
         PA_CUDA(c, cudaMemcpyAsync(&bad, &((PrepStats *)c->pstats.p)->bad_offsets, sizeof(bad),
                                    cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaMemcpyAsync(ranges, c->ranges.p, sizeof(ranges), cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaMemcpyAsync(counts, c->counts.p, 4 * kClasses, cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaStreamSynchronize(st));
         if (bad)
             return fail(c, PA_ERR_INVALID_ARGUMENT,
                         "offsets decrease or run past seq1_bytes / seq2_bytes; no pair was aligned");
     }
+    // Predicted bands (modes 1 and 2) are tried on long pairs only, the block and cluster classes
+    // (m * n at least the CTA threshold, 2^20 by default).  On shorter pairs the full DP of the
+    // short-pair kernel is faster than the band machinery can save (their predicted bands cover
+    // most of the matrix anyway), so they go straight to the full DP; a batch without long pairs
+    // skips the band prediction altogether.  Caller-given bands are tried on every pair.
+    const bool short_full = h_bands == nullptr;
+    const uint32_t n_long = counts[K_S16L] + counts[K_S32L] + counts[K_S16H] + counts[K_S32H];
     BandSpec *spec = (BandSpec *)c->band_spec.p;
-    if (h_bands) {
+    if (short_full && n_long == 0) {
+        // nothing to band
+    } else if (h_bands) {
         if ((s = ensure(c, c->band_in, np * 40))) return s;
         PA_CUDA(c, cudaMemcpyAsync(c->band_in.p, h_bands, np * 40, cudaMemcpyHostToDevice, st));
         band_from_ints_launch(st, (const int32_t *)c->band_in.p, np, spec);
@@ -717,10 +729,6 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     } else if ((s = band_predict(c, P, s1, o1, s2, o2, np, spec))) {
         return s;
     }
-    uint32_t ranges[16], counts[16];
-    PA_CUDA(c, cudaMemcpyAsync(ranges, c->ranges.p, sizeof(ranges), cudaMemcpyDeviceToHost, st));
-    PA_CUDA(c, cudaMemcpyAsync(counts, c->counts.p, 4 * kClasses, cudaMemcpyDeviceToHost, st));
-    PA_CUDA(c, cudaStreamSynchronize(st));
     // the largest pairs go to clusters only when their units fit in two waves of clusters
     if (c->ring.p) {
         const int slots = dp_cluster_grid(true, false, M_BAND, c->ring_grid) / kClusterBlocks;
@@ -813,10 +821,13 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     uint32_t *tmp = (uint32_t *)c->band_list[3 * NB].p, *redo = (uint32_t *)c->band_list[3 * NB + 1].p;
     uint32_t ncur[NB], nfull[NB] = {};
     for (int k = 0; k < NB; ++k) {
-        ncur[k] = counts[bc[k].klass];
-        if (ncur[k])
-            PA_CUDA(c, cudaMemcpyAsync(cur[k], (const uint32_t *)c->order.p + ranges[bc[k].klass], ncur[k] * 4ull,
-                                       cudaMemcpyDeviceToDevice, st));
+        const uint32_t cnt = counts[bc[k].klass];
+        const bool to_full = short_full && bc[k].kind == 0;     // short pairs: no band rounds
+        ncur[k] = to_full ? 0 : cnt;
+        if (to_full) nfull[k] = cnt;
+        if (cnt)
+            PA_CUDA(c, cudaMemcpyAsync(to_full ? full[k] : cur[k], (const uint32_t *)c->order.p + ranges[bc[k].klass],
+                                       cnt * 4ull, cudaMemcpyDeviceToDevice, st));
     }
     uint64_t banded = 0, rounds = 0;
     uint8_t *code = (uint8_t *)c->band_code.p;
