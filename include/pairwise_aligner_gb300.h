@@ -284,14 +284,19 @@ pa_status pa_set_substitution_matrix(pa_ctx *ctx, const uint8_t *symbols, uint32
  * proves its score or the band doubles; a pair whose band would cover more
  * than full_frac of its matrix, or that is still open after max_rounds, is
  * computed by the full DP.  margin scales the learned starting width;
- * straight_w0 is the starting width of band_mode 2. */
+ * straight_w0 is the starting width of band_mode 2.  Pairs of at most
+ * pa_set_team_threshold rows use team_full_frac instead of full_frac (0: full_frac):
+ * their full DP runs on teams of 4 warps, fast enough that a band pays only when it
+ * is much narrower than the matrix.  The full DP of long pairs is routed as in the
+ * plain path (teams, whole blocks, clusters, at the same time). */
 typedef struct pa_band_options {
     float margin;               /* default 1.25 */
     int32_t w_min;              /* default 16   */
     int32_t straight_w0;        /* default 64   */
     float full_frac;            /* default 0.5  */
     int32_t max_rounds;         /* default 6    */
-    int32_t reserved[3];
+    float team_full_frac;       /* default 0.5  */
+    int32_t reserved[2];
 } pa_band_options;
 
 pa_status pa_set_band_options(pa_ctx *ctx, const pa_band_options *options);

@@ -99,7 +99,8 @@ class PaBandOptions(ctypes.Structure):
         ("straight_w0", ctypes.c_int32),
         ("full_frac", ctypes.c_float),
         ("max_rounds", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 3),
+        ("team_full_frac", ctypes.c_float),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
 

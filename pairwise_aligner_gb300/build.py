@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libpa_gb300.so")
-SOURCES = ["pa_capi.cu", "pa_kern_v0.cu", "pa_kern_v1.cu", "pa_kern_v2.cu", "pa_kern_v3.cu", "pa_kern_v4.cu", "pa_kern_v5.cu", "pa_kern_v6.cu", "pa_kern_v7.cu", "pa_kern_v8.cu", "pa_kern_short_local.cu", "pa_kern_short_global.cu", "pa_kern_cta.cu", "pa_kern_cluster.cu", "pa_band_labels.cu", "pa_band.cu", "pa_band_dp.cu", "pa_static.cu", "pa_input.cu", "pa_traceback.cu"]
+SOURCES = ["pa_capi.cu", "pa_kern_v0.cu", "pa_kern_v1.cu", "pa_kern_v2.cu", "pa_kern_v3.cu", "pa_kern_v4.cu", "pa_kern_v5.cu", "pa_kern_v6.cu", "pa_kern_v7.cu", "pa_kern_v8.cu", "pa_kern_short_local.cu", "pa_kern_short_global.cu", "pa_kern_short_free.cu", "pa_kern_cta.cu", "pa_kern_cluster.cu", "pa_band_labels.cu", "pa_band.cu", "pa_band_dp.cu", "pa_static.cu", "pa_input.cu", "pa_traceback.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

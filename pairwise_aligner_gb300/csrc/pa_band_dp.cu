@@ -62,16 +62,22 @@ __device__ __forceinline__ int32_t half_width(const BandSpec &B, int32_t i, int3
     return (int32_t)(w > (1 << 30) ? (1 << 30) : w);
 }
 
-// One thread per listed pair: per-pass windows {first, last column} of the band
-// at width multiplier 2^shift, made monotone and overlapping like the DP kernel
-// does; code[k] = 2 when the windows cover more than full_frac of the matrix.
+// One warp per listed pair: per-pass windows {first, last column} of the band at width
+// multiplier 2^shift, made monotone and overlapping like the DP kernel does; code[k] = 2 when
+// the windows cover more than full_frac of the matrix (team_frac for pairs of at most
+// team_max_n rows).  The lanes take 32 columns at a time:
+// a warp scan gives the running maximum of the band's top (the first column that reaches a
+// pass) and, going back from column m, the running minimum of its bottom (the last column
+// that still reaches a pass); each pass boundary is written by the one lane that crosses it.
 __global__ void k_band_windows(const uint64_t *__restrict__ off1, const uint64_t *__restrict__ off2,
                                const uint32_t *__restrict__ list, uint32_t count, const BandSpec *__restrict__ spec,
-                               int32_t rows, int shift, float full_frac, int2 *__restrict__ win,
-                               uint8_t *__restrict__ code, unsigned long long *__restrict__ width_stats)
+                               int32_t rows, int shift, float full_frac, float team_frac, int32_t team_max_n,
+                               int2 *__restrict__ win, uint8_t *__restrict__ code,
+                               unsigned long long *__restrict__ width_stats)
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
+    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (k >= count) return;                       // whole warps: count is per warp
     const uint32_t id = list[k];
     const int32_t m = (int32_t)(off1[id + 1] - off1[id]), n = (int32_t)(off2[id + 1] - off2[id]);
     const BandSpec B = spec[id];
@@ -80,31 +86,61 @@ __global__ void k_band_windows(const uint64_t *__restrict__ off1, const uint64_t
     const int32_t dend = n - m;
     Centre C;
     C.init(B, m, n);
-    // first column of pass p: the first i whose band top (prefix maximum) reaches row p*rows+1
-    int seg = 0, p = 0;
-    int64_t top = INT64_MIN;
-    for (int32_t i = 1; i <= m && p < P; ++i) {
-        const int32_t c = C.at(i, seg), w = half_width(B, i, m, shift);
-        const int64_t hi = (int64_t)max(c, i + dend) + w;
-        top = hi > top ? hi : top;
-        while (p < P && (int64_t)p * rows + 1 <= top) wv[p++].x = i;
+    // passes p with p * rows + 1 <= v (the top v reaches them)
+    auto reached = [&](int64_t v) -> int32_t {
+        if (v < 1) return 0;
+        const int64_t q = (v - 1) / rows + 1;
+        return q < P ? (int32_t)q : P;
+    };
+    // the first pass p with min((p + 1) * rows, n) >= v (a bottom v reaches it and every later one)
+    auto first_reached = [&](int64_t v) -> int32_t {
+        if (v > n) return P;
+        if (v <= 0) return 0;
+        const int64_t q = (v + rows - 1) / rows - 1;
+        return q < P ? (int32_t)q : P;
+    };
+    int seg = 0;
+    int64_t top = INT64_MIN;                      // running maximum before this chunk
+    for (int32_t base = 1; base <= m && reached(top) < P; base += 32) {
+        const int32_t i = base + lane;
+        int64_t hi = INT64_MIN;
+        if (i <= m) hi = (int64_t)max(C.at(i, seg), i + dend) + half_width(B, i, m, shift);
+        int64_t run = max(hi, top);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, run, o);
+            if (lane >= o) run = max(run, y);
+        }
+        int64_t before = __shfl_up_sync(0xffffffffu, run, 1);
+        if (lane == 0) before = top;
+        for (int32_t p = reached(before); p < reached(run); ++p) wv[p].x = i;
+        top = __shfl_sync(0xffffffffu, run, 31);
     }
-    for (; p < P; ++p) wv[p].x = m;
-    // last column of pass p: the last i whose band bottom (suffix minimum) is at or above its last row
+    for (int32_t p = reached(top) + lane; p < P; p += 32) wv[p].x = m;
     seg = 8;
-    p = P - 1;
-    int64_t bot = INT64_MAX;
-    for (int32_t i = m; i >= 1 && p >= 0; --i) {
-        const int32_t c = C.at(i, seg), w = half_width(B, i, m, shift);
-        const int64_t lo = (int64_t)min(c, i + dend) - w;
-        bot = lo < bot ? lo : bot;
-        while (p >= 0 && bot <= (int64_t)min((p + 1) * rows, n)) wv[p--].y = i;
+    int64_t bot = INT64_MAX;                      // running minimum after this chunk
+    for (int32_t base = m; base >= 1 && first_reached(bot) > 0; base -= 32) {
+        const int32_t i = base - lane;
+        int64_t lo = INT64_MAX;
+        if (i >= 1) lo = (int64_t)min(C.at(i, seg), i + dend) - half_width(B, i, m, shift);
+        int64_t run = min(lo, bot);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, run, o);
+            if (lane >= o) run = min(run, y);
+        }
+        int64_t before = __shfl_up_sync(0xffffffffu, run, 1);
+        if (lane == 0) before = bot;
+        for (int32_t p = first_reached(run); p < first_reached(before); ++p) wv[p].y = i;
+        bot = __shfl_sync(0xffffffffu, run, 31);
     }
-    for (; p >= 0; --p) wv[p].y = 1;
+    for (int32_t p = lane; p < first_reached(bot); p += 32) wv[p].y = 1;
+    __syncwarp();
+    if (lane != 0) return;
     // the same monotone, overlapping fix-up as the DP kernel; cells of the result
     int64_t cells = 0;
     int32_t pa = 1, pb = 1;
-    for (p = 0; p < P; ++p) {
+    for (int32_t p = 0; p < P; ++p) {
         int2 x = wv[p];
         if (p == 0) x.x = 1;
         else x.x = max(min(x.x, pb), pa);
@@ -115,12 +151,27 @@ __global__ void k_band_windows(const uint64_t *__restrict__ off1, const uint64_t
         pa = x.x;
         pb = x.y;
     }
-    const bool full = (double)cells > (double)full_frac * (double)m * (double)n;
+    const float frac = (n <= team_max_n && team_frac > 0.f) ? team_frac : full_frac;
+    const bool full = (double)cells > (double)frac * (double)m * (double)n;
     code[k] = full ? 2 : 0;
     if (!full && width_stats) {          // mean window width of the banded pairs (team size)
         atomicAdd(width_stats, (unsigned long long)(cells / rows));
         atomicAdd(width_stats + 1, (unsigned long long)P);
     }
+}
+
+// The full DP's work kind of each listed pair, as the plain path's classifier routes long
+// pairs: 2 clusters (m * n >= huge_cells and n >= huge_min_n), 0 teams of 4 warps (at most
+// team_max_n rows), 1 whole blocks.
+__global__ void k_size_code(const uint64_t *__restrict__ off1, const uint64_t *__restrict__ off2,
+                            const uint32_t *__restrict__ list, uint32_t count, int32_t team_max_n, int64_t huge_cells,
+                            int32_t huge_min_n, uint8_t *__restrict__ code)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t id = list[k];
+    const int64_t m = (int64_t)(off1[id + 1] - off1[id]), n = (int64_t)(off2[id + 1] - off2[id]);
+    code[k] = (m * n >= huge_cells && n >= huge_min_n) ? 2 : (n <= team_max_n ? 0 : 1);
 }
 
 // Network outputs (16 floats per pair, 9 used) -> band: checkpoint diagonals
@@ -314,11 +365,22 @@ void band_dp_launch(bool lanes16, bool cta, int grid, cudaStream_t st, const DpL
 // width_stats (2 device words, may be null) accumulates the window widths and passes of
 // the pairs that stay banded.
 void band_windows_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, const uint32_t *list,
-                         uint32_t count, const BandSpec *spec, int32_t rows, int shift, float full_frac, int2 *win,
-                         uint8_t *code, unsigned long long *width_stats)
+                         uint32_t count, const BandSpec *spec, int32_t rows, int shift, float full_frac,
+                         float team_frac, int32_t team_max_n, int2 *win, uint8_t *code,
+                         unsigned long long *width_stats)
 {
-    if (count) k_band_windows<<<blocks(count, 128), 128, 0, st>>>(off1, off2, list, count, spec, rows, shift,
-                                                                   full_frac, win, code, width_stats);
+    // one warp per pair
+    if (count)
+        k_band_windows<<<blocks((uint64_t)count * 32, 128), 128, 0, st>>>(
+            off1, off2, list, count, spec, rows, shift, full_frac, team_frac, team_max_n, win, code, width_stats);
+}
+
+void size_code_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, const uint32_t *list,
+                      uint32_t count, int32_t team_max_n, int64_t huge_cells, int32_t huge_min_n, uint8_t *code)
+{
+    if (count)
+        k_size_code<<<blocks(count, 256), 256, 0, st>>>(off1, off2, list, count, team_max_n, huge_cells, huge_min_n,
+                                                         code);
 }
 
 void band_decode_launch(cudaStream_t st, const float *out, const uint64_t *off1, const uint64_t *off2,

@@ -94,7 +94,7 @@ struct pa_ctx {
     uint64_t graph_clock = 0;
     uint64_t last_launches = 0;
     // band mode
-    pa_band_options band_opt{1.25f, 16, 64, 0.5f, 6, {0, 0, 0}};
+    pa_band_options band_opt{1.25f, 16, 64, 0.5f, 6, 0.5f, {0, 0}};
     DevBuf band_spec, band_win, band_code, band_bsum, band_ctr, band_in;
     DevBuf band_list[20];
     DevBuf mlp_w[6], mlp_feat, mlp_x, mlp_h1, mlp_h2, mlp_out;
@@ -213,6 +213,7 @@ pa_status check_config(pa_ctx *c, const pa_config *cfg, DpParams &P, ClassCfg &C
     C.huge_min_n = c->huge_min_n;
     C.team_max_n = c->team_max_n;
     C.long_max_m = c->ring.p ? c->ring_m : 0;
+    C.qtab_s16 = 1;
     return PA_OK;
 }
 
@@ -247,19 +248,22 @@ void unpack_2bit_launch(const uint32_t *words, uint64_t first_base, uint64_t n, 
 
 int dp_short_occupancy_local(int G, int form);
 void dp_short_launch_local(int G, int form, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
-int dp_short_occupancy_global(int G, int form, bool free_ends);
-void dp_short_launch_global(int G, int form, bool free_ends, int grid, cudaStream_t st, const DpLaunch &L,
-                            const DpParams &P);
+int dp_short_occupancy_global(int G, int form);
+void dp_short_launch_global(int G, int form, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
+int dp_short_occupancy_free(int G);
+void dp_short_launch_free(int G, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
 
 int dp_short_occupancy(int G, int form, int mode)
 {
-    return mode == M_LOCAL ? dp_short_occupancy_local(G, form) : dp_short_occupancy_global(G, form, mode == M_GLOBAL_FREE);
+    return mode == M_LOCAL ? dp_short_occupancy_local(G, form)
+         : mode == M_GLOBAL ? dp_short_occupancy_global(G, form) : dp_short_occupancy_free(G);
 }
 
 void dp_short_launch(int G, int form, int mode, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
 {
     if (mode == M_LOCAL) dp_short_launch_local(G, form, grid, st, L, P);
-    else dp_short_launch_global(G, form, mode == M_GLOBAL_FREE, grid, st, L, P);
+    else if (mode == M_GLOBAL) dp_short_launch_global(G, form, grid, st, L, P);
+    else dp_short_launch_free(G, grid, st, L, P);
 }
 
 int dp_occupancy(int variant, bool lanes16, bool gen, int mode)
@@ -283,8 +287,11 @@ int band_dp_occupancy(bool lanes16, bool cta);
 int band_cta_occupancy();
 void band_dp_launch(bool lanes16, bool cta, int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P);
 void band_windows_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, const uint32_t *list,
-                         uint32_t count, const BandSpec *spec, int32_t rows, int shift, float full_frac, int2 *win,
-                         uint8_t *code, unsigned long long *width_stats);
+                         uint32_t count, const BandSpec *spec, int32_t rows, int shift, float full_frac,
+                         float team_frac, int32_t team_max_n, int2 *win, uint8_t *code,
+                         unsigned long long *width_stats);
+void size_code_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, const uint32_t *list,
+                      uint32_t count, int32_t team_max_n, int64_t huge_cells, int32_t huge_min_n, uint8_t *code);
 void band_decode_launch(cudaStream_t st, const float *out, const uint64_t *off1, const uint64_t *off2,
                         uint64_t n_pairs, const DpParams &P, float margin, int32_t w_min, BandSpec *spec);
 void band_straight_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, uint64_t n_pairs,
@@ -840,7 +847,8 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         const BandClass &B = bc[k];
         unsigned long long *wstat = (unsigned long long *)(ctr + 36);
         PA_CUDA(c, cudaMemsetAsync(wstat, 0, 16, st));
-        band_windows_launch(st, o1, o2, list, count, spec, B.rows, r, full_frac, (int2 *)c->band_win.p, code, wstat);
+        band_windows_launch(st, o1, o2, list, count, spec, B.rows, r, full_frac, c->band_opt.team_full_frac,
+                            c->team_max_n, (int2 *)c->band_win.p, code, wstat);
         compact_launch(st, list, code, count, 2, bsum, full[k] + nfull[k], ctr + 1);
         compact_launch(st, list, code, count, 0, bsum, tmp, ctr + 2);
         c->last_launches += 7;
@@ -916,8 +924,81 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         hc[k] = nfull[k];
     }
     PA_CUDA(c, cudaMemcpyAsync(ctr + 6, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
-    for (int k = 0; k < NB; ++k)
+    for (int k = 0; k < 2; ++k)                      // group classes
         if (nfull[k] && (s = full_dp(k, full[k], ctr + 6 + k, ctr + 16 + k))) return s;
+    // Long classes: the full DP routed as the plain path routes it -- teams of 4 warps for pairs
+    // of at most team_max_n rows, clusters for the largest pairs when their units fit in two
+    // waves of clusters (else whole blocks take them first), whole blocks for the rest -- the
+    // three kinds at the same time, on the call's two side streams.
+    for (int l = 0; l < 2; ++l) {
+        const int kl = 2 + l, kh = 4 + l;
+        const uint32_t total = nfull[kl] + nfull[kh];
+        if (!total) continue;
+        const bool lanes16 = l == 0;
+        uint32_t *all = cur[kl], *lc = cur[kh], *lb = nxt[kl], *lt = nxt[kh];   // free after the rounds
+        // the largest pairs first: the cluster-class list, then the block-class list
+        if (nfull[kh]) PA_CUDA(c, cudaMemcpyAsync(all, full[kh], nfull[kh] * 4ull, cudaMemcpyDeviceToDevice, st));
+        if (nfull[kl])
+            PA_CUDA(c, cudaMemcpyAsync(all + nfull[kh], full[kl], nfull[kl] * 4ull, cudaMemcpyDeviceToDevice, st));
+        uint32_t *cnt = ctr + 40 + 3 * l, *queue = ctr + 48 + 3 * l;
+        size_code_launch(st, o1, o2, all, total, c->team_max_n, c->huge_cells, c->huge_min_n, code);
+        compact_launch(st, all, code, total, 2, bsum, lc, cnt + 0);
+        compact_launch(st, all, code, total, 1, bsum, lb, cnt + 1);
+        compact_launch(st, all, code, total, 0, bsum, lt, cnt + 2);
+        c->last_launches += 10;
+        uint32_t h[3];
+        PA_CUDA(c, cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaStreamSynchronize(st));
+        DpLaunch F = L;
+        F.begin_ptr = ctr + 0;
+        F.rerun = 0;
+        F.team = 0;
+        F.G = 32;
+        F.rerun_list = (uint32_t *)c->rerun_long.p;
+        F.rerun_count = counters + 6;
+        const int slots = dp_cluster_grid(lanes16, false, M_GLOBAL, c->ring_grid) / kClusterBlocks;
+        const uint32_t cl_units = lanes16 ? (h[0] + 1) / 2 : h[0];
+        const bool clusters = h[0] > 0 && slots > 0 && cl_units <= 2u * (uint32_t)slots;
+        PA_CUDA(c, cudaEventRecord(c->ev_fork, st));
+        if (clusters) {
+            PA_CUDA(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+            DpLaunch FC = F;
+            FC.order = lc;
+            FC.count_ptr = cnt + 0;
+            FC.unit_counter = queue + 0;
+            FC.ring = cluster_ring(c);
+            PA_CUDA(c, dp_cluster_launch(lanes16, false, M_GLOBAL,
+                                         dp_cluster_grid(lanes16, false, M_GLOBAL, c->ring_grid), c->side, FC, P));
+            PA_CUDA(c, cudaEventRecord(c->ev_join, c->side));
+            c->last_launches++;
+        }
+        if (h[2]) {
+            PA_CUDA(c, cudaStreamWaitEvent(c->side2, c->ev_fork, 0));
+            DpLaunch FT = F;
+            FT.order = lt;
+            FT.count_ptr = cnt + 2;
+            FT.unit_counter = queue + 2;
+            FT.ring = team_ring(c);
+            dp_team_launch(lanes16, false, M_GLOBAL, c->ring_grid, c->side2, FT, P);
+            PA_CUDA(c, cudaEventRecord(c->ev_join2, c->side2));
+            c->last_launches++;
+        }
+        if (h[1] || (h[0] && !clusters)) {
+            DpLaunch FB = F;
+            FB.order = lb;
+            FB.count_ptr = cnt + 1;
+            FB.unit_counter = queue + 1;
+            if (h[0] && !clusters) {                  // the largest pairs ahead of the block list
+                FB.lead_order = lc;
+                FB.lead_begin_ptr = ctr + 0;
+                FB.lead_count_ptr = cnt + 0;
+            }
+            dp_cta_launch(lanes16, false, M_GLOBAL, c->ring_grid, st, FB, P);
+            c->last_launches++;
+        }
+        if (clusters) PA_CUDA(c, cudaStreamWaitEvent(st, c->ev_join, 0));
+        if (h[2]) PA_CUDA(c, cudaStreamWaitEvent(st, c->ev_join2, 0));
+    }
     if (nfull[0]) {                                   // s16 group results that failed their check
         DpLaunch F = L;
         F.order = (const uint32_t *)c->rerun.p;
@@ -1003,6 +1084,9 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
     ClassCfg C;
     s = check_config(c, cfg, P, C);
     if (s) return s;
+    // local pairs of the s16x2 class that the short-pair kernel takes (launch_class) never go
+    // back to dp_kernel (no s32 redo in local mode): the kernel builds its own column tables
+    if (P.local && c->variant[K_S16] >= kShortVariant && dp_short_supports(c->G[K_S16])) C.qtab_s16 = 0;
     if (n_pairs == 0) {
         if (stats) std::memset(stats, 0, sizeof(*stats));
         return PA_OK;
@@ -1344,7 +1428,7 @@ pa_status pa_set_band_options(pa_ctx *ctx, const pa_band_options *o)
 {
     if (!ctx || !o) return PA_ERR_INVALID_ARGUMENT;
     if (!(o->margin > 0.f) || o->w_min < 1 || o->straight_w0 < 1 || !(o->full_frac > 0.f) || o->max_rounds < 0 ||
-        o->max_rounds > 30)
+        o->max_rounds > 30 || !(o->team_full_frac >= 0.f))
         return fail(ctx, PA_ERR_INVALID_ARGUMENT, "band options out of range");
     ctx->band_opt = *o;
     return PA_OK;

@@ -22,6 +22,7 @@ struct ClassCfg {
     int32_t long_max_m;      // the longest sequence1 the ring rows hold
     int32_t huge_min_n;
     int32_t team_max_n;      // CTA-mode pairs with n at most this run on teams of 4 warps (0: none)
+    int32_t qtab_s16;        // write class K_S16's score tables (0: its kernel builds its own)
     const int8_t *rank_map;  // substitution-matrix scoring: symbol -> rank (null: unitary scores)
 };
 
@@ -150,8 +151,8 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
             klass += (m * n >= C.huge_cells && n >= C.huge_min_n) ? kHugeOffset
                      : (n <= C.team_max_n)                        ? kMediumOffset
                                                                   : kLongOffset;
-        if (klass == K_S16 || klass == K_S32 || klass == K_S16L || klass == K_S32L || klass == K_S16H ||
-            klass == K_S32H || klass == K_S16M || klass == K_S32M) {
+        if ((klass == K_S16 && C.qtab_s16) || klass == K_S32 || klass == K_S16L || klass == K_S32L ||
+            klass == K_S16H || klass == K_S32H || klass == K_S16M || klass == K_S32M) {
             uint32_t *qt = qtab + q0 + p;
             for (int64_t i = 4 * lane; i <= m; i += 128) {
                 const uint8_t *a = seq1 + q0 + i;

@@ -23,7 +23,8 @@ fixtures it writes are committed, so nothing on a GPU host reads the reference.
   from the matrix's symbol list, one-vs-many cases aligning the first sequence 1
   against every sequence 2.
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference]
+Usage: python tests/golden/make_golden.py --reference <reference checkout>
+(or PA_REFERENCE=<reference checkout> in the environment)
 """
 from __future__ import annotations
 
@@ -264,8 +265,11 @@ def oracle_cfg(c: dict, matrices: dict | None = None):
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("PA_REFERENCE"),
+                    help="the reference checkout (default: $PA_REFERENCE)")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("give --reference or set PA_REFERENCE")
     from oracle import oracle as O
 
     kats = parse_scalar_kats(args.reference)

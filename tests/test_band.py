@@ -338,3 +338,40 @@ def test_gpu_band_mode_rejects_local_and_free_ends():
         al = Aligner({**base, **change})
         with pytest.raises(PaError):
             al.compute([b"ACGTACGT"], [b"ACGTTCGT"])
+
+
+@pytest.mark.gpu
+def test_gpu_learned_band_gains_over_straight_band():
+    """What the network gains: on a fixed mixed-stream sample with 128-ish very long pairs
+    (20-50 kb, 6 % divergence, one or two 50-500 bp structural indels each), the trained
+    predictor's bands certify most very long pairs within one doubling.  Straight bands along
+    the main diagonal (band_mode 2, the same certificate and doubling) certify none of them
+    before they pass full_frac of the matrix.  Both modes return the plain path's results."""
+    import os
+    import torch
+    import pairwise_aligner_gb300 as pa
+    from pairwise_aligner_gb300 import Aligner, band
+    d = workloads.config5(seed=77, n_pairs=256, strata=(0.2, 0.3, 0.5))
+    very_long = d["stratum"] == 2
+    assert very_long.sum() >= 100
+    base = dict(local=False, match=d["match"], mismatch=d["mismatch"], gap_open=d["gap_open"],
+                gap_extension=d["gap_extension"], first_column_free=False, first_row_free=False,
+                last_column_free=False, last_row_free=False, band_mode=0)
+    args = (d["seq1"], d["off1"], d["seq2"], d["off2"])
+    plain = Aligner(base).compute_arrays(*args)
+    got = {}
+    for mode in (1, 2):
+        al = Aligner({**base, "band_mode": mode})
+        if mode == 1:
+            model = band.BandModel(device=torch.device("cuda:0"))
+            model.load(os.path.join(os.path.dirname(pa.__file__), "data", "band_model.npz"))
+            model.to_context(al.context)
+        res = al.compute_arrays(*args)
+        for f in ("score", "end1", "end2"):
+            assert np.array_equal(res[f], plain[f]), (mode, f)
+        got[mode] = res
+    cert = {k: ((r["flags"] & BANDED) != 0) & very_long for k, r in got.items()}
+    n_long = int(very_long.sum())
+    assert cert[1].sum() >= 0.6 * n_long, (int(cert[1].sum()), n_long)
+    assert cert[2].sum() <= 0.1 * n_long, (int(cert[2].sum()), n_long)
+    assert got[1]["band_rounds"][cert[1]].mean() <= 1.0        # round 0 or one doubling

@@ -93,3 +93,42 @@ def test_static_entry_rejects_sizes_beyond_its_scratch(env):
                                           dummy.data_ptr(), offs.data_ptr(), 16, 2, out.data_ptr(), None)
     assert rc == 8                               # PA_ERR_TOO_LARGE
     assert (out.cpu() == 0).all()
+
+
+def test_static_entry_flags_over_bound_and_empty_pairs(env, oracle):
+    """Per-pair flags: a pair whose scores could pass int32 (match 2^20 on 1,000 bases) gets
+    INT32_MIN and PA_RESULT_OVERFLOW from both device entries (the allocating one without a
+    stats block too); an empty global pair ("", "") carries the same flags and border result
+    from both entries, and the oracle's score."""
+    pa, _lib, lib, torch = env
+    from pairwise_aligner_gb300.aligner import Aligner
+    rng = np.random.default_rng(5)
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    a = acgt[rng.integers(0, 4, 1000)].tobytes()
+    pairs = [(a, a), (b"", b""), (b"ACGTAC", b"ACGAC"), (a[:40], a[:40])]
+    s1, o1 = pa.pack([p[0] for p in pairs])
+    s2, o2 = pa.pack([p[1] for p in pairs])
+    d = dict(seq1=s1, off1=o1, seq2=s2, off2=o2)
+    n = len(pairs)
+    t1, u1, t2, u2 = _device_batch(torch, d)
+    conf = dict(local=False, match=1 << 20, mismatch=-4, gap_open=-6, gap_extension=-1, first_column_free=0,
+                first_row_free=0, last_column_free=0, last_row_free=0, width_hint=0, band_mode=0)
+    al = Aligner(conf)
+    main = torch.zeros(n * 16, dtype=torch.uint8, device="cuda:0")
+    al.compute_device(t1, u1, t2, u2, main, stream=torch.cuda.current_stream(), stats=False)
+    torch.cuda.synchronize()
+    main = np.frombuffer(main.cpu().numpy().tobytes(), dtype=pa.RESULT_DTYPE)
+    out = torch.zeros(n * 16, dtype=torch.uint8, device="cuda:0")
+    rc = _static_call(lib, _lib, al.c_config(), t1, u1, t2, u2, out, n, None)
+    assert rc == 0, _lib.STATUS.get(rc, rc)
+    torch.cuda.synchronize()
+    got = np.frombuffer(out.cpu().numpy().tobytes(), dtype=pa.RESULT_DTYPE)
+    for res in (main, got):
+        assert res["score"][0] == np.iinfo(np.int32).min and res["flags"][0] & 0x10
+        assert not (res["flags"][1:] & 0x10).any()
+    assert got["flags"][1] == main["flags"][1] and got["flags"][1] & 0x08
+    oc = oracle.make_cfg(1 << 20, -4, -6, -1)
+    for k in (1, 2, 3):
+        want = oracle.align(oc, pairs[k][0], pairs[k][1])
+        for res in (main, got):
+            assert (int(res["score"][k]), int(res["end1"][k]), int(res["end2"][k])) == want, k
