@@ -26,7 +26,7 @@ One step = one call of the hot path over the whole batch:
             the checker here, never the thing timed (rank 0; a seeded sample when the
             batch is too large for the oracle to finish in about a minute).
   learned_band -- band mode 1 (the shipped predictor) against the plain full DP on the
-            16,384 held-out pairs of the learned-band workload and on a 65,536-pair
+            16,384 held-out pairs of the learned-band workload and on a 262,144-pair
             sample of the mixed global stream: GCUPS of both, certified pairs, band
             rounds, and whether the banded scores equal the plain ones.
 
@@ -457,7 +457,7 @@ def learned_band_section(dev, stream, args) -> dict:
     model = BD.BandModel(device=dev)
     model.load(BAND_MODEL)
     for name, d in (("config4_eval_16384_pairs", W.config4(seed=424242, n_pairs=16384)),
-                    ("config5_sample_65536_pairs", W.config5(seed=515151, n_pairs=65536))):
+                    ("config5_sample_262144_pairs", W.config5(seed=515151, n_pairs=262144))):
         cells = W.cells(d)
         n = len(d["off1"]) - 1
         s1 = torch.from_numpy(d["seq1"]).to(dev)

@@ -65,7 +65,6 @@ __device__ __forceinline__ void short_pass(const DpLaunch &L, const DpParams &P,
     const int32_t rows_full = G * R;
     const int32_t j0 = p * rows_full + t * RA;
     const uint32_t GOEA = V::cabs(P.gap_open + P.gap_ext);
-    const uint32_t NGOE = V::splat(P.gap_open + P.gap_ext);   // gap open + extend, negative
     const uint32_t EXTA = V::cabs(P.gap_ext);
     const uint32_t GOEH = SHIFTED ? V::cabs(P.gap_open + P.gap_ext - P.shift) : GOEA;
     const uint32_t EXTH = SHIFTED ? V::cabs(P.gap_ext - P.shift) : EXTA;
@@ -129,9 +128,7 @@ __device__ __forceinline__ void short_pass(const DpLaunch &L, const DpParams &P,
                 H[k] = h;
                 const uint32_t hoe = V::subc(h, GOEA);
                 Fr[k] = V::max2(V::subc(Fr[k], EXTH), SHIFTED ? V::subc(h, GOEH) : hoe);
-                // the vertical gap as one add-max on h: the row-to-row chain h -> gap -> h is
-                // two DPX operations, without the integer add of h - (open + extend) on it
-                Ed = V::addmax(h, NGOE, V::subc(Ed, EXTA));
+                Ed = V::max2(V::subc(Ed, EXTA), hoe);
                 tt = tn;
             }
             prevH = upH;
