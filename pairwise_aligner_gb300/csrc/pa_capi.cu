@@ -701,6 +701,28 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, st));
     PA_CUDA(c, cudaMemsetAsync(c->band_ctr.p, 0, 256, st));
     if ((s = enqueue_prep(c, P, C, s1, o1, b1, s2, o2, b2, out, np))) return s;
+    BandSpec *spec = (BandSpec *)c->band_spec.p;
+    DpLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.seq1 = s1; L.off1 = o1; L.seq2 = s2; L.off2 = o2;
+    L.qtab = (const uint32_t *)c->qtab.p;
+    L.out = out;
+    L.boundary = (Cell *)c->boundary.p;
+    L.slots = (Slot *)c->slots.p;
+    L.band_win = (const int2 *)c->band_win.p;
+    L.band = spec;
+    L.band_code = (uint8_t *)c->band_code.p;
+    L.dp_cells = (unsigned long long *)(ctr + 32);
+    L.ring = (Cell *)c->ring.p;
+    L.ring_stride = (uint64_t)c->ring_m + 2;
+    L.error = counters + 8;
+    L.spin_limit = c->wait_limit;
+    // Predicted bands (modes 1 and 2) are tried on long pairs only, the block and cluster classes
+    // (m * n at least the CTA threshold, 2^20 by default).  On shorter pairs the full DP of the
+    // short-pair kernel is faster than the band machinery can save (their predicted bands cover
+    // most of the matrix anyway), so they go straight to the full DP; a batch without long pairs
+    // skips the band prediction altogether.  Caller-given bands are tried on every pair.
+    const bool short_full = h_bands == nullptr;
     uint32_t ranges[16], counts[16];
     {
         // the classifier checked the offsets; a batch with inconsistent ones is not aligned (and
@@ -710,19 +732,32 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
                                    cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaMemcpyAsync(ranges, c->ranges.p, sizeof(ranges), cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaMemcpyAsync(counts, c->counts.p, 4 * kClasses, cudaMemcpyDeviceToHost, st));
-        PA_CUDA(c, cudaStreamSynchronize(st));
-        if (bad)
+        PA_CUDA(c, cudaEventRecord(c->ev_join, st));
+        if (short_full) {
+            // the group classes take the full DP whatever the counts: start it now from the
+            // device-side class ranges (as the plain path does), so that it runs while the host
+            // reads them; with offsets that failed the check the classes are empty
+            DpLaunch F = L;
+            F.order = (const uint32_t *)c->order.p;
+            F.rerun_list = (uint32_t *)c->rerun.p;
+            F.rerun_count = counters + 4;
+            const Klass gk[2] = {K_S16, K_S32};
+            for (int k = 0; k < 2; ++k) {
+                F.begin_ptr = (const uint32_t *)c->ranges.p + gk[k];
+                F.count_ptr = (const uint32_t *)c->counts.p + gk[k];
+                F.unit_counter = counters + k;
+                F.G = c->G[gk[k]];
+                launch_class(c, gk[k], M_GLOBAL, k == 0, false, F, P);
+            }
+        }
+        PA_CUDA(c, cudaEventSynchronize(c->ev_join));
+        if (bad) {
+            PA_CUDA(c, cudaStreamSynchronize(st));
             return fail(c, PA_ERR_INVALID_ARGUMENT,
                         "offsets decrease or run past seq1_bytes / seq2_bytes; no pair was aligned");
+        }
     }
-    // Predicted bands (modes 1 and 2) are tried on long pairs only, the block and cluster classes
-    // (m * n at least the CTA threshold, 2^20 by default).  On shorter pairs the full DP of the
-    // short-pair kernel is faster than the band machinery can save (their predicted bands cover
-    // most of the matrix anyway), so they go straight to the full DP; a batch without long pairs
-    // skips the band prediction altogether.  Caller-given bands are tried on every pair.
-    const bool short_full = h_bands == nullptr;
     const uint32_t n_long = counts[K_S16L] + counts[K_S32L] + counts[K_S16H] + counts[K_S32H];
-    BandSpec *spec = (BandSpec *)c->band_spec.p;
     if (short_full && n_long == 0) {
         // nothing to band
     } else if (h_bands) {
@@ -742,21 +777,6 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         if ((counts[K_S16H] + 1) / 2 + counts[K_S32H] > 2u * (uint32_t)slots) bc[4].kind = bc[5].kind = 1;
     }
 
-    DpLaunch L;
-    std::memset(&L, 0, sizeof(L));
-    L.seq1 = s1; L.off1 = o1; L.seq2 = s2; L.off2 = o2;
-    L.qtab = (const uint32_t *)c->qtab.p;
-    L.out = out;
-    L.boundary = (Cell *)c->boundary.p;
-    L.slots = (Slot *)c->slots.p;
-    L.band_win = (const int2 *)c->band_win.p;
-    L.band = spec;
-    L.band_code = (uint8_t *)c->band_code.p;
-    L.dp_cells = (unsigned long long *)(ctr + 32);
-    L.ring = (Cell *)c->ring.p;
-    L.ring_stride = (uint64_t)c->ring_m + 2;
-    L.error = counters + 8;
-    L.spin_limit = c->wait_limit;
     // the full DP of a list: group kernels (with the s16 -> s32 redo list), whole blocks or clusters
     auto full_dp = [&](int k, const uint32_t *list, uint32_t *count_word, uint32_t *queue) -> pa_status {
         DpLaunch F = L;
@@ -827,14 +847,18 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     }
     uint32_t *tmp = (uint32_t *)c->band_list[3 * NB].p, *redo = (uint32_t *)c->band_list[3 * NB + 1].p;
     uint32_t ncur[NB], nfull[NB] = {};
+    uint64_t short_pairs = 0;                         // group-class pairs already on the full DP
     for (int k = 0; k < NB; ++k) {
         const uint32_t cnt = counts[bc[k].klass];
-        const bool to_full = short_full && bc[k].kind == 0;     // short pairs: no band rounds
-        ncur[k] = to_full ? 0 : cnt;
-        if (to_full) nfull[k] = cnt;
+        if (short_full && bc[k].kind == 0) {          // short pairs: no band rounds (launched above)
+            ncur[k] = 0;
+            short_pairs += cnt;
+            continue;
+        }
+        ncur[k] = cnt;
         if (cnt)
-            PA_CUDA(c, cudaMemcpyAsync(to_full ? full[k] : cur[k], (const uint32_t *)c->order.p + ranges[bc[k].klass],
-                                       cnt * 4ull, cudaMemcpyDeviceToDevice, st));
+            PA_CUDA(c, cudaMemcpyAsync(cur[k], (const uint32_t *)c->order.p + ranges[bc[k].klass], cnt * 4ull,
+                                       cudaMemcpyDeviceToDevice, st));
     }
     uint64_t banded = 0, rounds = 0;
     uint8_t *code = (uint8_t *)c->band_code.p;
@@ -999,7 +1023,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         if (clusters) PA_CUDA(c, cudaStreamWaitEvent(st, c->ev_join, 0));
         if (h[2]) PA_CUDA(c, cudaStreamWaitEvent(st, c->ev_join2, 0));
     }
-    if (nfull[0]) {                                   // s16 group results that failed their check
+    if (nfull[0] || (short_full && counts[K_S16])) {  // s16 group results that failed their check
         DpLaunch F = L;
         F.order = (const uint32_t *)c->rerun.p;
         F.begin_ptr = counters + 5;
@@ -1036,6 +1060,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     st_out->dp_ms = st_out->device_ms;
     st_out->pairs_banded = banded;
     st_out->pairs_full_dp = counts[K_GEN] + counts[K_GENL] + counts[K_GENH];
+    st_out->pairs_full_dp += short_pairs;
     for (int k = 0; k < NB; ++k) st_out->pairs_full_dp += nfull[k];
     st_out->band_cells = cells;
     st_out->band_rounds = rounds;

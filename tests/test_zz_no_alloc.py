@@ -96,15 +96,16 @@ def test_static_entry_rejects_sizes_beyond_its_scratch(env):
 
 
 def test_static_entry_flags_over_bound_and_empty_pairs(env, oracle):
-    """Per-pair flags: a pair whose scores could pass int32 (match 2^20 on 1,000 bases) gets
-    INT32_MIN and PA_RESULT_OVERFLOW from both device entries (the allocating one without a
-    stats block too); an empty global pair ("", "") carries the same flags and border result
-    from both entries, and the oracle's score."""
+    """Per-pair flags: a pair over both entries' int32 bounds (match 2^20 on 1,100 bases; the
+    allocating entry's bound also counts the column shift of its s16 lanes, so it is the
+    stricter of the two) gets INT32_MIN and PA_RESULT_OVERFLOW from both device entries (the
+    allocating one without a stats block too); an empty global pair ("", "") carries the same
+    flags and border result from both entries, and the oracle's score."""
     pa, _lib, lib, torch = env
     from pairwise_aligner_gb300.aligner import Aligner
     rng = np.random.default_rng(5)
     acgt = np.frombuffer(b"ACGT", np.uint8)
-    a = acgt[rng.integers(0, 4, 1000)].tobytes()
+    a = acgt[rng.integers(0, 4, 1100)].tobytes()
     pairs = [(a, a), (b"", b""), (b"ACGTAC", b"ACGAC"), (a[:40], a[:40])]
     s1, o1 = pa.pack([p[0] for p in pairs])
     s2, o2 = pa.pack([p[1] for p in pairs])
