@@ -58,10 +58,11 @@ METRIC = "GCUPS (m*n cells/s), affine-gap local score DP + end coordinates, bit-
 METRIC_GLOBAL = "GCUPS (m*n cells/s), affine-gap global score DP, bit-exact"
 WORKLOAD = "config2_local_262144_pairs_64-512bp_+1/-4/-6/-1"
 BAND_MODEL = os.path.join(REPO, "pairwise_aligner_gb300", "data", "band_model.npz")
-# DRAM bytes per cell of the s16x2 local DP kernel, from one ncu capture of its launch on the
-# first 32,768 pairs of this workload (dram__bytes_read.sum + dram__bytes_write.sum divided by
-# the launch's 2.7146e9 cells; the traffic grows with the cells).
-DRAM_BYTES_PER_CELL = (49.772288e6 + 4.112896e6) / 2714564472
+# DRAM bytes per cell of the short-pair local DP kernel (dp_short, 8 lanes per group, 32 rows
+# per thread), from one ncu capture of its launch on all 262,144 pairs of this workload:
+# dram__bytes.sum.per_second (207.49 GB/s) x gpu__time_duration.sum (4.95712 ms) over the
+# launch's 2.1770e10 cells.  Most of it is the write-back of the 16-byte column slots.
+DRAM_BYTES_PER_CELL = 207.492454e9 * 4.957120e-3 / 21769527988
 
 
 def env_rank():
@@ -388,7 +389,8 @@ def our_arm(args):
                      "unit": "GCUPS", "frac": round(achieved / peak_gcups, 4),
                      "traffic": int(DRAM_BYTES_PER_CELL * cells) if args.workload == "config2" else None,
                      "peak_source": "pa_measure_roofline: whole-chip s16x2 cell-update instruction mix, measured live",
-                     "kernel": "dp_kernel<L16> (all DP kernels of one call)", "kernel_ms": round(dp_ms, 4),
+                     "kernel": "the DP kernels of one call (config 2: dp_short, s16x2, 8 lanes per group, "
+                               "32 rows per thread)", "kernel_ms": round(dp_ms, 4),
                      "hbm": {"achieved": round(alg_bytes / (dp_ms * 1e-3) / 1e9, 1),
                              "peak": hbm_peak(), "unit": "GB/s",
                              "frac": round(alg_bytes / (dp_ms * 1e-3) / 1e9 / hbm_peak(), 5)}},

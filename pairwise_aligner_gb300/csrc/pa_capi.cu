@@ -300,6 +300,8 @@ void band_from_ints_launch(cudaStream_t st, const int32_t *in, uint64_t n_pairs,
 void compact_launch(cudaStream_t st, const uint32_t *list, const uint8_t *code, uint32_t count, uint8_t sel,
                     uint32_t *block_sum, uint32_t *out, uint32_t *total);
 void mark_full_launch(cudaStream_t st, pa_result *out, uint64_t n_pairs);
+void any_long_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, uint64_t n_pairs, int64_t long_cells,
+                     int sm_count, uint32_t *flag);
 
 void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStream_t st, const DpLaunch &L,
                const DpParams &P)
@@ -366,7 +368,9 @@ pa_status enqueue_prep(pa_ctx *c, const DpParams &P, const ClassCfg &C, const ui
     PA_CUDA(c, cudaMemsetAsync(c->hist.p, 0, sizeof(uint32_t) * kBuckets, st));
     PA_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, st));
     PA_CUDA(c, cudaMemsetAsync(c->pstats.p, 0, sizeof(PrepStats), st));
-    int cls_blocks = (int)std::min<uint64_t>((n_pairs * 32 + 127) / 128, (uint64_t)c->sm_count * 128);
+    // one resident wave (16 blocks of 4 warps per SM), each warp a stride of pairs: every block
+    // adds its statistics to the same few global counters once, so fewer blocks contend less
+    int cls_blocks = (int)std::min<uint64_t>((n_pairs * 32 + 127) / 128, (uint64_t)c->sm_count * 16);
     if (cls_blocks < 1) cls_blocks = 1;
     k_classify<<<cls_blocks, 128, 0, st>>>(s1, o1, b1, s2, o2, b2, n_pairs, P, C, (uint32_t *)c->keys.p,
                                               (uint32_t *)c->hist.p, (uint32_t *)c->qtab.p, out,
@@ -647,6 +651,33 @@ pa_status band_predict(pa_ctx *c, const DpParams &P, const uint8_t *s1, const ui
 }
 
 pa_status read_stats(pa_ctx *c, pa_stats *stats);
+
+// The checks band mode makes of its configuration, then whether any pair is a candidate for
+// band rounds (m * n at least the block-mode threshold); any_long stays true when the check
+// cannot run (no pairs, null offsets: run_band reports those).
+pa_status band_gate(pa_ctx *c, const pa_config *cfg, const uint64_t *o1, const uint64_t *o2, uint64_t n_pairs,
+                    bool &any_long)
+{
+    any_long = true;
+    DpParams P;
+    ClassCfg C;
+    pa_status s = check_config(c, cfg, P, C);
+    if (s) return s;
+    if (P.local || P.first_column_free || P.first_row_free || P.last_column_free || P.last_row_free)
+        return fail(c, PA_ERR_UNSUPPORTED, "band mode needs global alignment with penalised end gaps");
+    if (cfg->band_mode == 1 && !c->has_model)
+        return fail(c, PA_ERR_INVALID_ARGUMENT, "band_mode 1 needs a band model (pa_set_band_model)");
+    if (n_pairs == 0 || n_pairs >= (1ull << 31) || !o1 || !o2) return PA_OK;
+    if ((s = ensure(c, c->band_ctr, 256))) return s;
+    uint32_t *flag = (uint32_t *)c->band_ctr.p + 63;
+    uint32_t h = 0;
+    PA_CUDA(c, cudaMemsetAsync(flag, 0, 4, c->stream));
+    any_long_launch(c->stream, o1, o2, n_pairs, c->long_cells, c->sm_count, flag);
+    PA_CUDA(c, cudaMemcpyAsync(&h, flag, 4, cudaMemcpyDeviceToHost, c->stream));
+    PA_CUDA(c, cudaStreamSynchronize(c->stream));
+    any_long = h != 0;
+    return PA_OK;
+}
 
 // Band mode (host-synchronous between rounds): classify and sort as the plain
 // path, build every pair's band, then per round and work class: windows ->
@@ -1101,7 +1132,27 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
                      const uint8_t *s2, const uint64_t *o2, uint64_t b2, uint64_t n_pairs, pa_result *out,
                      pa_stats *stats, bool sync_for_stats)
 {
-    if (cfg && cfg->band_mode) return run_band(c, cfg, s1, o1, b1, s2, o2, b2, n_pairs, out, nullptr, stats);
+    if (cfg && cfg->band_mode) {
+        // A band-mode batch without a pair of at least the block-mode size has nothing to band
+        // (predicted bands are tried on long pairs only): it aligns as the plain path does,
+        // graph replay included, and its results get the band path's PA_RESULT_FULL_DP.  One
+        // small kernel and a 4-byte read decide it.
+        bool any_long = true;
+        pa_status s = band_gate(c, cfg, o1, o2, n_pairs, any_long);
+        if (s) return s;
+        if (any_long) return run_band(c, cfg, s1, o1, b1, s2, o2, b2, n_pairs, out, nullptr, stats);
+        pa_config plain = *cfg;
+        plain.band_mode = 0;
+        if ((s = run_device(c, &plain, s1, o1, b1, s2, o2, b2, n_pairs, out, stats, sync_for_stats))) return s;
+        mark_full_launch(c->stream, out, n_pairs);
+        c->last_launches++;
+        PA_CUDA(c, cudaGetLastError());
+        if (stats) {
+            stats->pairs_full_dp = stats->pairs_s16 + stats->pairs_s32 + stats->pairs_general;
+            stats->kernel_launches = c->last_launches;
+        }
+        return PA_OK;
+    }
     apply_tuning(c, cfg, n_pairs, b1, b2);
     pa_status s = n_pairs ? ensure_ring(c, c->want_ring_m) : PA_OK;
     if (s) return s;
