@@ -379,7 +379,7 @@ def our_arm(args):
         "vs_baseline": None, "dtype": "int16x2 lanes (int32 where a pair needs it)", "data": "synthetic",
         "config": {"workload": workload_name(d, args.workload, n), "pairs": n, "cells": cells,
                    "group_threads": ctx_G(args), "band_mode": args.band,
-                   "l2": ("inputs (bytes + 4-byte score tables) larger than the 129 MB L2; no flush" if not small
+                   "l2": ("inputs (sequence bytes, per-column slots or score tables) larger than the 129 MB L2; no flush" if not small
                           else "inputs smaller than L2: a 256 MB buffer is written before every timed step"),
                    "pairs_s16": st["pairs_s16"], "pairs_s32": st["pairs_s32"], "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(replica_throughput(cells, e2e_s * 1e3, world), 2), "unit": "GCUPS",

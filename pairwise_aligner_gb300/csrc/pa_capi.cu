@@ -96,7 +96,7 @@ struct pa_ctx {
     // band mode
     pa_band_options band_opt{1.25f, 16, 64, 0.65f, 2, 0.65f, {0, 0}};
     DevBuf band_spec, band_win, band_code, band_bsum, band_ctr, band_in;
-    DevBuf band_list[20];
+    DevBuf band_list[22];
     DevBuf mlp_w[6], mlp_feat, mlp_x, mlp_h1, mlp_h2, mlp_out;
     bool has_model = false;
     // substitution matrix (PA_SCORE_MATRIX): int8 rank per byte (-1: not a symbol), int32 scores
@@ -895,55 +895,134 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     uint8_t *code = (uint8_t *)c->band_code.p;
     uint32_t *bsum = (uint32_t *)c->band_bsum.p;
     const float full_frac = c->band_opt.full_frac;
-    // one round of work class k over `list`: pairs to widen go to next, s16 results to redo
-    // in s32 to redo_out (or nowhere)
-    auto band_step = [&](int k, const uint32_t *list, uint32_t count, int r, bool rerun, uint32_t *next,
-                         uint32_t &n_next, uint32_t *redo_out, uint32_t &n_redo) -> pa_status {
-        const BandClass &B = bc[k];
-        unsigned long long *wstat = (unsigned long long *)(ctr + 36);
-        PA_CUDA(c, cudaMemsetAsync(wstat, 0, 16, st));
-        band_windows_launch(st, o1, o2, list, count, spec, B.rows, r, full_frac, c->band_opt.team_full_frac,
-                            c->team_max_n, (int2 *)c->band_win.p, code, wstat);
-        compact_launch(st, list, code, count, 2, bsum, full[k] + nfull[k], ctr + 1);
-        compact_launch(st, list, code, count, 0, bsum, tmp, ctr + 2);
+    // One round of work class k over `list`: pairs to widen go to `next`, s16 results to redo in
+    // s32 to `redo_out` (or nowhere).  A step has its own list, code, counter and stream slots,
+    // so that two steps can run their banded DP at the same time: open() queues the windows and
+    // their compaction, read() collects the counts (host wait), dp() launches the banded DP on
+    // the step's stream and ring rows, close() compacts its outcome, collect() reads it.
+    struct Step {
+        int k = 0;
+        const uint32_t *list = nullptr;
+        uint32_t count = 0;
+        bool rerun = false;
+        uint32_t *next = nullptr, *n_next = nullptr, *redo_out = nullptr;
+        uint32_t n_redo = 0;
+        uint32_t *tmpl = nullptr;                    // the pairs that run the banded DP
+        uint8_t *code = nullptr;                     // per list position
+        uint32_t *cw = nullptr;                      // 5 device words: full, banded, queue, widen, redo
+        unsigned long long *ws = nullptr;            // 2 device words: window cells, passes
+        cudaStream_t stream = nullptr;
+        Cell *ring = nullptr;
+        uint32_t nb = 0;
+        int team = 1;
+    };
+    const auto *opt = &c->band_opt;
+    auto step_open = [&](Step &S, int r) -> pa_status {
+        const BandClass &B = bc[S.k];
+        PA_CUDA(c, cudaMemsetAsync(S.ws, 0, 16, st));
+        band_windows_launch(st, o1, o2, S.list, S.count, spec, B.rows, r, full_frac, opt->team_full_frac,
+                            c->team_max_n, (int2 *)c->band_win.p, S.code, S.ws);
+        compact_launch(st, S.list, S.code, S.count, 2, bsum, full[S.k] + nfull[S.k], S.cw + 0);
+        compact_launch(st, S.list, S.code, S.count, 0, bsum, S.tmpl, S.cw + 1);
         c->last_launches += 7;
+        return PA_OK;
+    };
+    auto step_read = [&](Step &S) -> pa_status {
+        const BandClass &B = bc[S.k];
         uint32_t h[2];
-        unsigned long long ws[2];
-        PA_CUDA(c, cudaMemcpyAsync(h, ctr + 1, 8, cudaMemcpyDeviceToHost, st));
-        PA_CUDA(c, cudaMemcpyAsync(ws, wstat, 16, cudaMemcpyDeviceToHost, st));
+        unsigned long long w[2];
+        PA_CUDA(c, cudaMemcpyAsync(h, S.cw, 8, cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaMemcpyAsync(w, S.ws, 16, cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaStreamSynchronize(st));
-        nfull[k] += h[0];
-        const uint32_t nb = h[1];
-        if (nb == 0) return PA_OK;
+        nfull[S.k] += h[0];
+        S.nb = h[1];
         // CTA mode: a team of warps per pair sized to the passes a window keeps in flight
-        const double mean_width = ws[1] ? (double)ws[0] / (double)ws[1] : 0.0;
-        L.team = mean_width >= 8.0 * B.rows ? 8 : mean_width >= 4.0 * B.rows ? 4 : mean_width >= 2.0 * B.rows ? 2 : 1;
-        PA_CUDA(c, cudaMemsetAsync(ctr + 3, 0, 4, st));
-        L.order = tmp;
-        L.begin_ptr = ctr + 0;
-        L.count_ptr = ctr + 2;
-        L.unit_counter = ctr + 3;
-        L.G = B.kind ? 32 : c->G[B.klass];
-        L.band_rows = B.rows;
-        L.band_round = r;
-        L.rerun = rerun ? 1 : 0;
+        const double mean_width = w[1] ? (double)w[0] / (double)w[1] : 0.0;
+        S.team = mean_width >= 8.0 * B.rows ? 8 : mean_width >= 4.0 * B.rows ? 4 : mean_width >= 2.0 * B.rows ? 2 : 1;
+        return PA_OK;
+    };
+    auto step_dp = [&](Step &S, int r) -> pa_status {
+        if (S.nb == 0) return PA_OK;
+        const BandClass &B = bc[S.k];
+        DpLaunch LB = L;
+        PA_CUDA(c, cudaMemsetAsync(S.cw + 2, 0, 4, S.stream));
+        LB.team = S.team;
+        LB.order = S.tmpl;
+        LB.begin_ptr = ctr + 0;
+        LB.count_ptr = S.cw + 1;
+        LB.unit_counter = S.cw + 2;
+        LB.band_code = S.code;
+        LB.G = B.kind ? 32 : c->G[B.klass];
+        LB.band_rows = B.rows;
+        LB.band_round = r;
+        LB.rerun = S.rerun ? 1 : 0;
         if (B.kind == 2) {
-            DpLaunch LB = L;
             LB.ring = cluster_ring(c);
             PA_CUDA(c, dp_cluster_launch(B.lanes16, false, M_BAND, dp_cluster_grid(B.lanes16, false, M_BAND, c->ring_grid),
-                                         st, LB, P));
-        } else
+                                         S.stream, LB, P));
+        } else {
+            LB.ring = S.ring;
             band_dp_launch(B.lanes16, B.kind == 1,
-                           B.kind ? c->ring_grid : band_dp_occupancy(B.lanes16, false) * c->sm_count, st, L, P);
-        compact_launch(st, tmp, code, nb, 1, bsum, next + n_next, ctr + 4);
-        compact_launch(st, tmp, code, nb, 3, bsum, redo_out ? redo_out : tmp, ctr + 5);
-        c->last_launches += 7;
-        PA_CUDA(c, cudaMemcpyAsync(h, ctr + 4, 8, cudaMemcpyDeviceToHost, st));
+                           B.kind ? c->ring_grid : band_dp_occupancy(B.lanes16, false) * c->sm_count, S.stream, LB, P);
+        }
+        c->last_launches++;
+        return PA_OK;
+    };
+    auto step_close = [&](Step &S) -> pa_status {
+        if (S.nb == 0) return PA_OK;
+        compact_launch(st, S.tmpl, S.code, S.nb, 1, bsum, S.next + *S.n_next, S.cw + 3);
+        compact_launch(st, S.tmpl, S.code, S.nb, 3, bsum, S.redo_out ? S.redo_out : S.tmpl, S.cw + 4);
+        c->last_launches += 6;
+        return PA_OK;
+    };
+    auto step_collect = [&](Step &S) -> pa_status {
+        if (S.nb == 0) return PA_OK;
+        uint32_t h[2];
+        PA_CUDA(c, cudaMemcpyAsync(h, S.cw + 3, 8, cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaStreamSynchronize(st));
         PA_CUDA(c, cudaGetLastError());
-        n_next += h[0];
-        n_redo = redo_out ? h[1] : 0;
-        banded += nb - h[0] - h[1];
+        *S.n_next += h[0];
+        S.n_redo = S.redo_out ? h[1] : 0;
+        banded += S.nb - h[0] - h[1];
+        return PA_OK;
+    };
+    uint32_t *tmp2 = (uint32_t *)c->band_list[3 * NB + 2].p, *redo2 = (uint32_t *)c->band_list[3 * NB + 3].p;
+    // slot 0: the call's stream and the block-mode ring rows; slot 1: the first side stream and
+    // the team region of the ring (cluster steps use the cluster region in either slot)
+    auto make_step = [&](int slot, int k, const uint32_t *list, uint32_t count, bool rerun, uint32_t *next,
+                         uint32_t *n_next, uint32_t *redo_out, uint32_t code_off) {
+        Step S;
+        S.k = k; S.list = list; S.count = count; S.rerun = rerun;
+        S.next = next; S.n_next = n_next; S.redo_out = redo_out;
+        S.tmpl = slot ? tmp2 : tmp;
+        S.code = code + code_off;
+        S.cw = slot ? ctr + 22 : ctr + 1;
+        S.ws = (unsigned long long *)(slot ? ctr + 28 : ctr + 36);
+        S.stream = slot ? c->side : st;
+        S.ring = slot ? team_ring(c) : (Cell *)c->ring.p;
+        return S;
+    };
+    // one step alone, on slot 0
+    auto band_step = [&](int k, const uint32_t *list, uint32_t count, int r, bool rerun, uint32_t *next,
+                         uint32_t &n_next, uint32_t *redo_out, uint32_t &n_redo) -> pa_status {
+        Step S = make_step(0, k, list, count, rerun, next, &n_next, redo_out, 0);
+        pa_status e;
+        if ((e = step_open(S, r)) || (e = step_read(S)) || (e = step_dp(S, r)) || (e = step_close(S)) ||
+            (e = step_collect(S)))
+            return e;
+        n_redo = S.n_redo;
+        return PA_OK;
+    };
+    // two steps whose banded DPs run at the same time (the long and the largest pairs)
+    auto band_pair = [&](Step &A, Step &B, int r) -> pa_status {
+        pa_status e;
+        if ((e = step_open(A, r)) || (e = step_open(B, r)) || (e = step_read(A)) || (e = step_read(B))) return e;
+        PA_CUDA(c, cudaEventRecord(c->ev_fork, st));
+        PA_CUDA(c, cudaStreamWaitEvent(B.stream, c->ev_fork, 0));
+        if ((e = step_dp(A, r)) || (e = step_dp(B, r))) return e;
+        PA_CUDA(c, cudaEventRecord(c->ev_join, B.stream));
+        PA_CUDA(c, cudaStreamWaitEvent(st, c->ev_join, 0));
+        if ((e = step_close(A)) || (e = step_close(B)) || (e = step_collect(A)) || (e = step_collect(B))) return e;
         return PA_OK;
     };
     auto open_pairs = [&]() {
@@ -951,17 +1030,34 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         for (int k = 0; k < NB; ++k) t += ncur[k];
         return t;
     };
-    for (int r = 0; r < c->band_opt.max_rounds && open_pairs(); ++r) {
+    for (int r = 0; r < opt->max_rounds && open_pairs(); ++r) {
         ++rounds;
         uint32_t nn[NB] = {};
-        for (int k16 : {0, 2, 4}) {                   // s16 classes, then their s32 redo, then s32
-            uint32_t nredo = 0, none = 0;
-            if (ncur[k16] && (s = band_step(k16, cur[k16], ncur[k16], r, false, nxt[k16], nn[k16], redo, nredo)))
+        uint32_t nredo[NB] = {}, none = 0;
+        uint32_t *redo_of[NB] = {redo, nullptr, redo, nullptr, redo2, nullptr};
+        // the s16 group class (caller-given bands only), then its s32 redo and the s32 groups
+        if (ncur[0] && (s = band_step(0, cur[0], ncur[0], r, false, nxt[0], nn[0], redo, nredo[0]))) return s;
+        if (nredo[0] && (s = band_step(1, redo, nredo[0], r, true, nxt[1], nn[1], nullptr, none))) return s;
+        if (ncur[1] && (s = band_step(1, cur[1], ncur[1], r, false, nxt[1], nn[1], nullptr, none))) return s;
+        // the s16 long and largest classes: both banded DPs at once when both have pairs
+        if (ncur[2] && ncur[4]) {
+            Step A = make_step(0, 2, cur[2], ncur[2], false, nxt[2], &nn[2], redo_of[2], 0);
+            Step B = make_step(1, 4, cur[4], ncur[4], false, nxt[4], &nn[4], redo_of[4], ncur[2]);
+            if ((s = band_pair(A, B, r))) return s;
+            nredo[2] = A.n_redo;
+            nredo[4] = B.n_redo;
+        } else {
+            for (int k16 : {2, 4})
+                if (ncur[k16] &&
+                    (s = band_step(k16, cur[k16], ncur[k16], r, false, nxt[k16], nn[k16], redo_of[k16], nredo[k16])))
+                    return s;
+        }
+        for (int k16 : {2, 4}) {                      // their s32 redo, then the s32 classes
+            if (nredo[k16] && (s = band_step(k16 + 1, redo_of[k16], nredo[k16], r, true, nxt[k16 + 1], nn[k16 + 1],
+                                             nullptr, none)))
                 return s;
-            if (nredo && (s = band_step(k16 + 1, redo, nredo, r, true, nxt[k16 + 1], nn[k16 + 1], nullptr, none)))
-                return s;
-            if (ncur[k16 + 1] &&
-                (s = band_step(k16 + 1, cur[k16 + 1], ncur[k16 + 1], r, false, nxt[k16 + 1], nn[k16 + 1], nullptr, none)))
+            if (ncur[k16 + 1] && (s = band_step(k16 + 1, cur[k16 + 1], ncur[k16 + 1], r, false, nxt[k16 + 1],
+                                                nn[k16 + 1], nullptr, none)))
                 return s;
         }
         for (int k = 0; k < NB; ++k) {

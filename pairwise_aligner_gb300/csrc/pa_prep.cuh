@@ -95,8 +95,12 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint32_t match4 = (uint8_t)(P.match - P.shift) * 0x01010101u;     // scores of H - shift * column
     const uint32_t mis4 = (uint8_t)(P.mismatch - P.shift) * 0x01010101u;
-    // statistics are summed per lane 0 and per block, then added once per block
-    unsigned long long my_cells = 0, my_class[16] = {}, my_overflow = 0, my_bad = 0;
+    // statistics: per lane 0 in registers (cells, overflow, bad offsets) and per block in
+    // shared memory (class sizes), added to the global counters once per block
+    __shared__ unsigned long long sh[19];
+    if (threadIdx.x < 19) sh[threadIdx.x] = 0;
+    __syncthreads();
+    unsigned long long my_cells = 0, my_overflow = 0, my_bad = 0;
     for (uint64_t p = warp; p < n_pairs; p += nwarps) {
         const uint64_t q0 = off1[p], q1 = off1[p + 1], t0 = off2[p], t1 = off2[p + 1];
         if (q0 > q1 || q1 > seq1_bytes || t0 > t1 || t1 > seq2_bytes) {
@@ -109,6 +113,7 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
         }
         const int64_t m = (int64_t)(q1 - q0), n = (int64_t)(t1 - t0);
         bool dna = true;
+#pragma unroll 4
         for (int64_t j = 4 * lane; j < n; j += 128) {     // four independent loads per lane
             const uint8_t *q = seq2 + t0 + j;
             const int64_t left = n - j;
@@ -180,16 +185,11 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
             }
             keys[p] = key;
             atomicAdd(&hist[key], 1u);
-            ++my_class[klass];
+            atomicAdd(&sh[1 + klass], 1ull);
         }
     }
-    __shared__ unsigned long long sh[19];
-    if (threadIdx.x < 19) sh[threadIdx.x] = 0;
-    __syncthreads();
     if (lane == 0) {
         if (my_cells) atomicAdd(&sh[0], my_cells);
-        for (int k = 0; k < 16; ++k)
-            if (my_class[k]) atomicAdd(&sh[1 + k], my_class[k]);
         if (my_overflow) atomicAdd(&sh[17], my_overflow);
         if (my_bad) atomicAdd(&sh[18], my_bad);
     }
