@@ -70,6 +70,9 @@ struct pa_ctx {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaStream_t side2 = nullptr;                     // team kernels run beside the CTA kernels
     cudaEvent_t ev_join2 = nullptr;
+    uint32_t *pinned = nullptr;                       // small page-locked host words (band gate)
+    uint32_t gate_gen = 0;                            // call number the band gate's flag is keyed to
+    void *gate_buf = nullptr;                         // the buffer whose flag word was last cleared
     pa_options opt{};
     std::string err;
     // device work buffers (grow only)
@@ -94,7 +97,7 @@ struct pa_ctx {
     uint64_t graph_clock = 0;
     uint64_t last_launches = 0;
     // band mode
-    pa_band_options band_opt{1.25f, 16, 64, 0.65f, 2, 0.65f, {0, 0}};
+    pa_band_options band_opt{1.25f, 16, 64, 0.75f, 2, 0.65f, {0, 0}};
     DevBuf band_spec, band_win, band_code, band_bsum, band_ctr, band_in;
     DevBuf band_list[22];
     DevBuf mlp_w[6], mlp_feat, mlp_x, mlp_h1, mlp_h2, mlp_out;
@@ -301,7 +304,7 @@ void compact_launch(cudaStream_t st, const uint32_t *list, const uint8_t *code, 
                     uint32_t *block_sum, uint32_t *out, uint32_t *total);
 void mark_full_launch(cudaStream_t st, pa_result *out, uint64_t n_pairs);
 void any_long_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, uint64_t n_pairs, int64_t long_cells,
-                     int sm_count, uint32_t *flag);
+                     int sm_count, uint32_t tag, uint32_t *flag);
 
 void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStream_t st, const DpLaunch &L,
                const DpParams &P)
@@ -669,13 +672,18 @@ pa_status band_gate(pa_ctx *c, const pa_config *cfg, const uint64_t *o1, const u
         return fail(c, PA_ERR_INVALID_ARGUMENT, "band_mode 1 needs a band model (pa_set_band_model)");
     if (n_pairs == 0 || n_pairs >= (1ull << 31) || !o1 || !o2) return PA_OK;
     if ((s = ensure(c, c->band_ctr, 256))) return s;
+    // the kernel writes this call's number into the flag word when it finds a long pair, so
+    // the word is cleared only for a new buffer or when the numbers wrap
     uint32_t *flag = (uint32_t *)c->band_ctr.p + 63;
-    uint32_t h = 0;
-    PA_CUDA(c, cudaMemsetAsync(flag, 0, 4, c->stream));
-    any_long_launch(c->stream, o1, o2, n_pairs, c->long_cells, c->sm_count, flag);
-    PA_CUDA(c, cudaMemcpyAsync(&h, flag, 4, cudaMemcpyDeviceToHost, c->stream));
+    if (++c->gate_gen == 0 || c->gate_buf != c->band_ctr.p) {
+        PA_CUDA(c, cudaMemsetAsync(flag, 0, 4, c->stream));
+        c->gate_buf = c->band_ctr.p;
+        if (c->gate_gen == 0) c->gate_gen = 1;
+    }
+    any_long_launch(c->stream, o1, o2, n_pairs, c->long_cells, c->sm_count, c->gate_gen, flag);
+    PA_CUDA(c, cudaMemcpyAsync(c->pinned, flag, 4, cudaMemcpyDeviceToHost, c->stream));
     PA_CUDA(c, cudaStreamSynchronize(c->stream));
-    any_long = h != 0;
+    any_long = *(volatile uint32_t *)c->pinned == c->gate_gen;
     return PA_OK;
 }
 
@@ -1408,9 +1416,10 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
         cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaHostAlloc((void **)&c->pinned, 64, cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
-        delete c;
+        pa_destroy(c);
         return PA_ERR_CUDA;
     }
     // defaults measured on GB300 (262,144 pairs of 64..512 bp): local s16x2 is fastest with
@@ -1467,6 +1476,7 @@ pa_status pa_destroy(pa_ctx *c)
     if (c->side) cudaStreamDestroy(c->side);
     if (c->side2) cudaStreamDestroy(c->side2);
     if (c->ev_join2) cudaEventDestroy(c->ev_join2);
+    if (c->pinned) cudaFreeHost(c->pinned);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return PA_OK;
@@ -1663,14 +1673,8 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
     }
     if ((packed ? (!words1 || !words2) : (!seq1 || !seq2)) || !off1 || !off2 || !out)
         return fail(ctx, PA_ERR_INVALID_ARGUMENT, "null buffer");
-    int64_t long_m = 0;
-    for (uint64_t k = 0; k < n_pairs; ++k) {
-        if (off1[k + 1] < off1[k] || off2[k + 1] < off2[k])
-            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "offsets must be non-decreasing");
-        const int64_t m = (int64_t)(off1[k + 1] - off1[k]), n = (int64_t)(off2[k + 1] - off2[k]);
-        if (m * n >= ctx->long_cells) long_m = std::max(long_m, m);
-    }
-    ctx->want_ring_m = long_m;      // exact: the ring rows hold the longest CTA-mode sequence1
+    if (off1[n_pairs] < off1[0] || off2[n_pairs] < off2[0])
+        return fail(ctx, PA_ERR_INVALID_ARGUMENT, "offsets must be non-decreasing");
     if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, PA_ERR_CUDA, "cudaSetDevice");
     // the device copies hold bytes [0, off[n]) with offsets rebased to 0
     const uint64_t base1 = off1[0], base2 = off2[0];
@@ -1713,6 +1717,18 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
     PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off2.p, h2, (n_pairs + 1) * 8, cudaMemcpyHostToDevice, st));
     PA_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
     PA_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
+    // the offsets' check and the longest block-mode sequence1 (ring-row size), while the copies
+    // above run; nothing is launched on the copied bytes before the check passes
+    int64_t long_m = 0;
+    for (uint64_t k = 0; k < n_pairs; ++k) {
+        if (off1[k + 1] < off1[k] || off2[k + 1] < off2[k]) {
+            PA_CUDA(ctx, cudaStreamSynchronize(st));
+            return fail(ctx, PA_ERR_INVALID_ARGUMENT, "offsets must be non-decreasing");
+        }
+        const int64_t m = (int64_t)(off1[k + 1] - off1[k]), n = (int64_t)(off2[k + 1] - off2[k]);
+        if (m * n >= ctx->long_cells) long_m = std::max(long_m, m);
+    }
+    ctx->want_ring_m = long_m;      // exact: the ring rows hold the longest CTA-mode sequence1
     if (config && config->band_mode) {
         s = run_band(ctx, config, (const uint8_t *)ctx->in_seq1.p, (const uint64_t *)ctx->in_off1.p, b1,
                      (const uint8_t *)ctx->in_seq2.p, (const uint64_t *)ctx->in_off2.p, b2, n_pairs,
