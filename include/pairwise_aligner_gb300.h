@@ -159,7 +159,9 @@ pa_status pa_align_batch(pa_ctx *ctx, const pa_config *config,
  * PA_ERR_OVERFLOW, PA_ERR_TIMEOUT, symbols outside a substitution matrix) are
  * returned as a status only when stats is non-NULL (the call then waits for the
  * device); without stats the call returns as soon as the work is queued, and the
- * affected pairs carry PA_RESULT_OVERFLOW / PA_RESULT_ERROR in their results. */
+ * affected pairs carry PA_RESULT_OVERFLOW / PA_RESULT_ERROR in their results.
+ * Band mode waits on the host for the class counts and for every band round; without
+ * stats it returns once its last launches are queued. */
 pa_status pa_align_batch_device(pa_ctx *ctx, const pa_config *config,
                                 const uint8_t *d_seq1, const uint64_t *d_off1, uint64_t seq1_bytes,
                                 const uint8_t *d_seq2, const uint64_t *d_off2, uint64_t seq2_bytes,

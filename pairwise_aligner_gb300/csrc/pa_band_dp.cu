@@ -174,21 +174,6 @@ __global__ void k_size_code(const uint64_t *__restrict__ off1, const uint64_t *_
     code[k] = (m * n >= huge_cells && n >= huge_min_n) ? 2 : (n <= team_max_n ? 0 : 1);
 }
 
-// flag = tag when some pair has m * n >= long_cells (a candidate for band rounds), or lengths
-// that only decreasing offsets give (the band path reports those).
-__global__ void k_any_long(const uint64_t *__restrict__ off1, const uint64_t *__restrict__ off2, uint64_t n_pairs,
-                           int64_t long_cells, uint32_t tag, uint32_t *__restrict__ flag)
-{
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n_pairs; k += stride) {
-        const uint64_t m = off1[k + 1] - off1[k], n = off2[k + 1] - off2[k];
-        if (m >= (1ull << 31) || n >= (1ull << 31) || (int64_t)(m * n) >= long_cells) {
-            *flag = tag;
-            return;
-        }
-    }
-}
-
 // Network outputs (16 floats per pair, 9 used) -> band: checkpoint diagonals
 // out[c] * (m + n) / 4 and, from the predicted deficit c2 = 2^(16 out[8]) - 1
 // (= smax (m + n) - 2 S), the starting half-width.  A path that leaves the band
@@ -424,14 +409,6 @@ void compact_launch(cudaStream_t st, const uint32_t *list, const uint8_t *code, 
     if (nb) k_compact_count<<<nb, 1024, 0, st>>>(code, count, sel, block_sum);
     k_compact_scan<<<1, 1024, 0, st>>>(block_sum, nb, total);
     if (nb) k_compact_write<<<nb, 1024, 0, st>>>(list, code, count, sel, block_sum, out);
-}
-
-void any_long_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, uint64_t n_pairs, int64_t long_cells,
-                     int sm_count, uint32_t tag, uint32_t *flag)
-{
-    if (n_pairs)
-        k_any_long<<<(unsigned)std::min<uint64_t>(blocks(n_pairs, 256), (uint64_t)sm_count * 8), 256, 0, st>>>(
-            off1, off2, n_pairs, long_cells, tag, flag);
 }
 
 void mark_full_launch(cudaStream_t st, pa_result *out, uint64_t n_pairs)

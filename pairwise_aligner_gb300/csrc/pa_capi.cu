@@ -33,6 +33,7 @@ namespace {
 constexpr int kR = 16;             // rows per thread per lane
 constexpr int64_t kDefaultRingM = 65536;   // device entry points: CTA mode up to this sequence1 length
 constexpr int kDefaultG = 8;       // threads per group
+constexpr size_t kPinnedBytes = 1024;   // band mode's host reads (counts, per-step totals)
 constexpr int kShortVariant = 9;   // variants 9, 10: dp_short (s16x2 unitary short pairs), 16 / 32 rows per thread
 constexpr int kVariants = kShortVariant + kShortFormCount;   // 0..8: dp_kernel (pa_kern_v*.cu)
 constexpr int kDefaultShortVariant = kShortVariant;          // with the rule below: 16 or 32 rows per thread
@@ -70,9 +71,7 @@ struct pa_ctx {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaStream_t side2 = nullptr;                     // team kernels run beside the CTA kernels
     cudaEvent_t ev_join2 = nullptr;
-    uint32_t *pinned = nullptr;                       // small page-locked host words (band gate)
-    uint32_t gate_gen = 0;                            // call number the band gate's flag is keyed to
-    void *gate_buf = nullptr;                         // the buffer whose flag word was last cleared
+    uint8_t *pinned = nullptr;                        // page-locked host words for band mode's reads
     pa_options opt{};
     std::string err;
     // device work buffers (grow only)
@@ -303,8 +302,6 @@ void band_from_ints_launch(cudaStream_t st, const int32_t *in, uint64_t n_pairs,
 void compact_launch(cudaStream_t st, const uint32_t *list, const uint8_t *code, uint32_t count, uint8_t sel,
                     uint32_t *block_sum, uint32_t *out, uint32_t *total);
 void mark_full_launch(cudaStream_t st, pa_result *out, uint64_t n_pairs);
-void any_long_launch(cudaStream_t st, const uint64_t *off1, const uint64_t *off2, uint64_t n_pairs, int64_t long_cells,
-                     int sm_count, uint32_t tag, uint32_t *flag);
 
 void dp_launch(int variant, bool lanes16, bool gen, int mode, int grid, cudaStream_t st, const DpLaunch &L,
                const DpParams &P)
@@ -655,45 +652,13 @@ pa_status band_predict(pa_ctx *c, const DpParams &P, const uint8_t *s1, const ui
 
 pa_status read_stats(pa_ctx *c, pa_stats *stats);
 
-// The checks band mode makes of its configuration, then whether any pair is a candidate for
-// band rounds (m * n at least the block-mode threshold); any_long stays true when the check
-// cannot run (no pairs, null offsets: run_band reports those).
-pa_status band_gate(pa_ctx *c, const pa_config *cfg, const uint64_t *o1, const uint64_t *o2, uint64_t n_pairs,
-                    bool &any_long)
-{
-    any_long = true;
-    DpParams P;
-    ClassCfg C;
-    pa_status s = check_config(c, cfg, P, C);
-    if (s) return s;
-    if (P.local || P.first_column_free || P.first_row_free || P.last_column_free || P.last_row_free)
-        return fail(c, PA_ERR_UNSUPPORTED, "band mode needs global alignment with penalised end gaps");
-    if (cfg->band_mode == 1 && !c->has_model)
-        return fail(c, PA_ERR_INVALID_ARGUMENT, "band_mode 1 needs a band model (pa_set_band_model)");
-    if (n_pairs == 0 || n_pairs >= (1ull << 31) || !o1 || !o2) return PA_OK;
-    if ((s = ensure(c, c->band_ctr, 256))) return s;
-    // the kernel writes this call's number into the flag word when it finds a long pair, so
-    // the word is cleared only for a new buffer or when the numbers wrap
-    uint32_t *flag = (uint32_t *)c->band_ctr.p + 63;
-    if (++c->gate_gen == 0 || c->gate_buf != c->band_ctr.p) {
-        PA_CUDA(c, cudaMemsetAsync(flag, 0, 4, c->stream));
-        c->gate_buf = c->band_ctr.p;
-        if (c->gate_gen == 0) c->gate_gen = 1;
-    }
-    any_long_launch(c->stream, o1, o2, n_pairs, c->long_cells, c->sm_count, c->gate_gen, flag);
-    PA_CUDA(c, cudaMemcpyAsync(c->pinned, flag, 4, cudaMemcpyDeviceToHost, c->stream));
-    PA_CUDA(c, cudaStreamSynchronize(c->stream));
-    any_long = *(volatile uint32_t *)c->pinned == c->gate_gen;
-    return PA_OK;
-}
-
 // Band mode (host-synchronous between rounds): classify and sort as the plain
 // path, build every pair's band, then per round and work class: windows ->
 // (too wide: full-DP list) -> banded DP -> certified results, pairs to widen,
 // and s16 results to redo in s32; finally the full DP for what is left.
 pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uint64_t *o1, uint64_t b1,
                    const uint8_t *s2, const uint64_t *o2, uint64_t b2, uint64_t n_pairs, pa_result *out,
-                   const int32_t *h_bands, pa_stats *stats)
+                   const int32_t *h_bands, pa_stats *stats, bool sync_at_end)
 {
     apply_tuning(c, cfg, n_pairs, b1, b2);
     pa_status s = n_pairs ? ensure_ring(c, c->want_ring_m) : PA_OK;
@@ -762,15 +727,17 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     // most of the matrix anyway), so they go straight to the full DP; a batch without long pairs
     // skips the band prediction altogether.  Caller-given bands are tried on every pair.
     const bool short_full = h_bands == nullptr;
+    // page-locked host words: the copies below do not wait for the stream, so the group
+    // classes' full DP is queued before the host waits for the class counts
+    unsigned long long *h_bad = (unsigned long long *)c->pinned;
+    uint32_t *h_ranges = (uint32_t *)(c->pinned + 16), *h_counts = (uint32_t *)(c->pinned + 80);
     uint32_t ranges[16], counts[16];
     {
         // the classifier checked the offsets; a batch with inconsistent ones is not aligned (and
         // the band features, which read the sequences, must not run on it)
-        unsigned long long bad = 0;
-        PA_CUDA(c, cudaMemcpyAsync(&bad, &((PrepStats *)c->pstats.p)->bad_offsets, sizeof(bad),
-                                   cudaMemcpyDeviceToHost, st));
-        PA_CUDA(c, cudaMemcpyAsync(ranges, c->ranges.p, sizeof(ranges), cudaMemcpyDeviceToHost, st));
-        PA_CUDA(c, cudaMemcpyAsync(counts, c->counts.p, 4 * kClasses, cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaMemcpyAsync(h_bad, &((PrepStats *)c->pstats.p)->bad_offsets, 8, cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaMemcpyAsync(h_ranges, c->ranges.p, 64, cudaMemcpyDeviceToHost, st));
+        PA_CUDA(c, cudaMemcpyAsync(h_counts, c->counts.p, 4 * kClasses, cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaEventRecord(c->ev_join, st));
         if (short_full) {
             // the group classes take the full DP whatever the counts: start it now from the
@@ -790,7 +757,9 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
             }
         }
         PA_CUDA(c, cudaEventSynchronize(c->ev_join));
-        if (bad) {
+        std::memcpy(ranges, h_ranges, sizeof(ranges));
+        std::memcpy(counts, h_counts, 4 * kClasses);
+        if (*h_bad) {
             PA_CUDA(c, cudaStreamSynchronize(st));
             return fail(c, PA_ERR_INVALID_ARGUMENT,
                         "offsets decrease or run past seq1_bytes / seq2_bytes; no pair was aligned");
@@ -921,6 +890,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         unsigned long long *ws = nullptr;            // 2 device words: window cells, passes
         cudaStream_t stream = nullptr;
         Cell *ring = nullptr;
+        size_t pin = 0;                              // its page-locked host words (32 bytes)
         uint32_t nb = 0;
         int team = 1;
     };
@@ -937,8 +907,8 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     };
     auto step_read = [&](Step &S) -> pa_status {
         const BandClass &B = bc[S.k];
-        uint32_t h[2];
-        unsigned long long w[2];
+        uint32_t *h = (uint32_t *)(c->pinned + S.pin);
+        unsigned long long *w = (unsigned long long *)(c->pinned + S.pin + 8);
         PA_CUDA(c, cudaMemcpyAsync(h, S.cw, 8, cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaMemcpyAsync(w, S.ws, 16, cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaStreamSynchronize(st));
@@ -985,7 +955,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     };
     auto step_collect = [&](Step &S) -> pa_status {
         if (S.nb == 0) return PA_OK;
-        uint32_t h[2];
+        uint32_t *h = (uint32_t *)(c->pinned + S.pin + 24);
         PA_CUDA(c, cudaMemcpyAsync(h, S.cw + 3, 8, cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaStreamSynchronize(st));
         PA_CUDA(c, cudaGetLastError());
@@ -1007,6 +977,7 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         S.cw = slot ? ctr + 22 : ctr + 1;
         S.ws = (unsigned long long *)(slot ? ctr + 28 : ctr + 36);
         S.stream = slot ? c->side : st;
+        S.pin = slot ? 192 : 160;
         S.ring = slot ? team_ring(c) : (Cell *)c->ring.p;
         return S;
     };
@@ -1082,7 +1053,13 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         nfull[k] += ncur[k];
         hc[k] = nfull[k];
     }
-    PA_CUDA(c, cudaMemcpyAsync(ctr + 6, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
+    bool any_full = false;
+    for (int k = 0; k < NB; ++k) any_full |= nfull[k] != 0;
+    if (any_full) {
+        uint32_t *h_hc = (uint32_t *)(c->pinned + 256);
+        std::memcpy(h_hc, hc, sizeof(hc));
+        PA_CUDA(c, cudaMemcpyAsync(ctr + 6, h_hc, sizeof(hc), cudaMemcpyHostToDevice, st));
+    }
     for (int k = 0; k < 2; ++k)                      // group classes
         if (nfull[k] && (s = full_dp(k, full[k], ctr + 6 + k, ctr + 16 + k))) return s;
     // Long classes: the full DP routed as the plain path routes it -- teams of 4 warps for pairs
@@ -1105,8 +1082,8 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         compact_launch(st, all, code, total, 1, bsum, lb, cnt + 1);
         compact_launch(st, all, code, total, 0, bsum, lt, cnt + 2);
         c->last_launches += 10;
-        uint32_t h[3];
-        PA_CUDA(c, cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+        uint32_t *h = (uint32_t *)(c->pinned + 224);
+        PA_CUDA(c, cudaMemcpyAsync(h, cnt, 12, cudaMemcpyDeviceToHost, st));
         PA_CUDA(c, cudaStreamSynchronize(st));
         DpLaunch F = L;
         F.begin_ptr = ctr + 0;
@@ -1182,6 +1159,12 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     mark_full_launch(st, out, np);
     c->last_launches++;
     PA_CUDA(c, cudaEventRecord(c->ev1, st));
+    if (!sync_at_end) {
+        // like the plain device entry without stats: the call returns once the work is queued,
+        // and errors found on the device are in the pairs' results
+        PA_CUDA(c, cudaGetLastError());
+        return PA_OK;
+    }
     PA_CUDA(c, cudaStreamSynchronize(st));
     PA_CUDA(c, cudaGetLastError());
     unsigned long long cells = 0;
@@ -1236,27 +1219,8 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
                      const uint8_t *s2, const uint64_t *o2, uint64_t b2, uint64_t n_pairs, pa_result *out,
                      pa_stats *stats, bool sync_for_stats)
 {
-    if (cfg && cfg->band_mode) {
-        // A band-mode batch without a pair of at least the block-mode size has nothing to band
-        // (predicted bands are tried on long pairs only): it aligns as the plain path does,
-        // graph replay included, and its results get the band path's PA_RESULT_FULL_DP.  One
-        // small kernel and a 4-byte read decide it.
-        bool any_long = true;
-        pa_status s = band_gate(c, cfg, o1, o2, n_pairs, any_long);
-        if (s) return s;
-        if (any_long) return run_band(c, cfg, s1, o1, b1, s2, o2, b2, n_pairs, out, nullptr, stats);
-        pa_config plain = *cfg;
-        plain.band_mode = 0;
-        if ((s = run_device(c, &plain, s1, o1, b1, s2, o2, b2, n_pairs, out, stats, sync_for_stats))) return s;
-        mark_full_launch(c->stream, out, n_pairs);
-        c->last_launches++;
-        PA_CUDA(c, cudaGetLastError());
-        if (stats) {
-            stats->pairs_full_dp = stats->pairs_s16 + stats->pairs_s32 + stats->pairs_general;
-            stats->kernel_launches = c->last_launches;
-        }
-        return PA_OK;
-    }
+    if (cfg && cfg->band_mode)
+        return run_band(c, cfg, s1, o1, b1, s2, o2, b2, n_pairs, out, nullptr, stats, sync_for_stats || stats);
     apply_tuning(c, cfg, n_pairs, b1, b2);
     pa_status s = n_pairs ? ensure_ring(c, c->want_ring_m) : PA_OK;
     if (s) return s;
@@ -1417,7 +1381,7 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
         cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-        cudaHostAlloc((void **)&c->pinned, 64, cudaHostAllocDefault) != cudaSuccess) {
+        cudaHostAlloc((void **)&c->pinned, kPinnedBytes, cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         pa_destroy(c);
         return PA_ERR_CUDA;
@@ -1732,7 +1696,7 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
     if (config && config->band_mode) {
         s = run_band(ctx, config, (const uint8_t *)ctx->in_seq1.p, (const uint64_t *)ctx->in_off1.p, b1,
                      (const uint8_t *)ctx->in_seq2.p, (const uint64_t *)ctx->in_off2.p, b2, n_pairs,
-                     (pa_result *)ctx->in_out.p, bands, stats);
+                     (pa_result *)ctx->in_out.p, bands, stats, true);
         if (s && s != PA_ERR_OVERFLOW) return s;
         PA_CUDA(ctx, cudaMemcpyAsync(out, ctx->in_out.p, n_pairs * sizeof(pa_result), cudaMemcpyDeviceToHost, st));
         PA_CUDA(ctx, cudaStreamSynchronize(st));
