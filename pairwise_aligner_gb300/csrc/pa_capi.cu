@@ -650,7 +650,8 @@ pa_status band_predict(pa_ctx *c, const DpParams &P, const uint8_t *s1, const ui
     return PA_OK;
 }
 
-pa_status read_stats(pa_ctx *c, pa_stats *stats);
+pa_status read_stats(pa_ctx *c, pa_stats *stats, bool staged = false);
+void stage_stats(pa_ctx *c, cudaStream_t st);
 
 // Band mode (host-synchronous between rounds): classify and sort as the plain
 // path, build every pair's band, then per round and work class: windows ->
@@ -1185,13 +1186,28 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     return s;
 }
 
+// Queue the copies of the call's counters into page-locked host words (read_stats with
+// staged = true reads them after the caller's wait on `st`).
+constexpr size_t kPinStats = 512;      // PrepStats, then 16 counter words
+void stage_stats(pa_ctx *c, cudaStream_t st)
+{
+    static_assert(kPinStats + sizeof(PrepStats) + 64 <= kPinnedBytes, "page-locked words");
+    cudaMemcpyAsync(c->pinned + kPinStats, c->pstats.p, sizeof(PrepStats), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->pinned + kPinStats + sizeof(PrepStats), c->counters.p, 64, cudaMemcpyDeviceToHost, st);
+}
+
 // Counters of the finished call (after a sync): class sizes, reruns, error bits.
-pa_status read_stats(pa_ctx *c, pa_stats *stats)
+pa_status read_stats(pa_ctx *c, pa_stats *stats, bool staged)
 {
     PrepStats ps;
     uint32_t ctr[16];
-    PA_CUDA(c, cudaMemcpy(&ps, c->pstats.p, sizeof(ps), cudaMemcpyDeviceToHost));
-    PA_CUDA(c, cudaMemcpy(ctr, c->counters.p, sizeof(ctr), cudaMemcpyDeviceToHost));
+    if (staged) {
+        std::memcpy(&ps, c->pinned + kPinStats, sizeof(ps));
+        std::memcpy(ctr, c->pinned + kPinStats + sizeof(PrepStats), sizeof(ctr));
+    } else {
+        PA_CUDA(c, cudaMemcpy(&ps, c->pstats.p, sizeof(ps), cudaMemcpyDeviceToHost));
+        PA_CUDA(c, cudaMemcpy(ctr, c->counters.p, sizeof(ctr), cudaMemcpyDeviceToHost));
+    }
     if (stats) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
@@ -1707,8 +1723,9 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
                    (pa_result *)ctx->in_out.p, stats, false);
     if (s) return s;
     PA_CUDA(ctx, cudaMemcpyAsync(out, ctx->in_out.p, n_pairs * sizeof(pa_result), cudaMemcpyDeviceToHost, st));
+    stage_stats(ctx, st);
     PA_CUDA(ctx, cudaStreamSynchronize(st));
-    return read_stats(ctx, stats);
+    return read_stats(ctx, stats, true);
 }
 
 // Traceback: inputs staged like pa_align_batch; pairs in chunks whose direction words fit

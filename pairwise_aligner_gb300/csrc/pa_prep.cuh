@@ -174,11 +174,10 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
                 out[p] = r;
                 key = (uint32_t)K_NONE << kClassShift;
             } else {
-                const int32_t rows = C.rows[klass], G = C.gcnt[klass], R = C.rpt[klass];
-                const int64_t passes = (n + rows - 1) / rows;
-                const int64_t rem = n - (passes - 1) * rows;
-                const int64_t nch = (rem + G * 4 - 1) / (G * 4);
-                const uint64_t shape = (uint64_t)(passes - 1) * (R / 4) + (uint64_t)(nch - 1);
+                // the pass shape, (passes - 1) * R/4 + (chunks of 4G rows in the last pass - 1), is
+                // ceil(n / 4G) - 1 because a pass holds G*R rows, a multiple of 4G; G is a power of two
+                const uint32_t G = (uint32_t)C.gcnt[klass];
+                const uint64_t shape = (uint64_t)(n - 1) >> (2 + (31 - __clz(G)));
                 key = (klass << kClassShift) | (quant_shape(shape > 0xffffffffull ? 0xffffffffu : (uint32_t)shape) << 10) |
                       quant_len((uint32_t)m);
                 my_cells += (unsigned long long)(m * n);
