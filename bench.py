@@ -391,6 +391,12 @@ def our_arm(args):
                      "peak_source": "pa_measure_roofline: whole-chip s16x2 cell-update instruction mix, measured live",
                      "kernel": "the DP kernels of one call (config 2: dp_short, s16x2, 8 lanes per group, "
                                "32 rows per thread)", "kernel_ms": round(dp_ms, 4),
+                     "local_mix": ({"peak": round(peak["s16x2_local_cells_per_s"] / 1e9, 1),
+                                    "frac": round(achieved / (peak["s16x2_local_cells_per_s"] / 1e9), 4),
+                                    "note": "the same mix plus local scoring's per-column maximum "
+                                            "(k_roofline<L16, TRACK>), for context; frac above is the one "
+                                            "against the recurrence alone"}
+                                   if d["local"] and peak.get("s16x2_local_cells_per_s") else None),
                      "hbm": {"achieved": round(alg_bytes / (dp_ms * 1e-3) / 1e9, 1),
                              "peak": hbm_peak(), "unit": "GB/s",
                              "frac": round(alg_bytes / (dp_ms * 1e-3) / 1e9 / hbm_peak(), 5)}},

@@ -373,6 +373,7 @@ typedef struct pa_roofline {
     double sm_clock_mhz;
     int32_t sm_count;
     int32_t reserved;
+    double s16x2_local_cells_per_s;   /* the s16x2 mix plus local scoring's column maximum */
 } pa_roofline;
 pa_status pa_measure_roofline(pa_ctx *ctx, pa_roofline *out);
 

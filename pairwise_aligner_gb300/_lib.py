@@ -155,6 +155,7 @@ class PaRoofline(ctypes.Structure):
         ("sm_clock_mhz", ctypes.c_double),
         ("sm_count", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
+        ("s16x2_local_cells_per_s", ctypes.c_double),
     ]
 
 

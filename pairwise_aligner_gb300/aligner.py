@@ -158,7 +158,8 @@ class Context:
         r = _lib.PaRoofline()
         _lib.check(self.lib.pa_measure_roofline(self.ptr, ctypes.byref(r)), self.ptr)
         return {"s16x2_cells_per_s": r.s16x2_cells_per_s, "s32_cells_per_s": r.s32_cells_per_s,
-                "sm_clock_mhz": r.sm_clock_mhz, "sm_count": r.sm_count}
+                "sm_clock_mhz": r.sm_clock_mhz, "sm_count": r.sm_count,
+                "s16x2_local_cells_per_s": r.s16x2_local_cells_per_s}
 
 
 RESULT_DTYPE = np.dtype([("score", np.int32), ("end1", np.int32), ("end2", np.int32), ("width", np.uint8),

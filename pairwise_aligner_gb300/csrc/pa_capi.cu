@@ -33,7 +33,12 @@ namespace {
 constexpr int kR = 16;             // rows per thread per lane
 constexpr int64_t kDefaultRingM = 65536;   // device entry points: CTA mode up to this sequence1 length
 constexpr int kDefaultG = 8;       // threads per group
-constexpr size_t kPinnedBytes = 1024;   // band mode's host reads (counts, per-step totals)
+// Page-locked host words of a context: [0, 8) band mode's bad-offset count, [16, 80) class
+// ranges, [80, 144) class counts, [160, 224) the two band steps' totals, [224, 236) the long
+// full-DP routing counts, [256, 280) full-DP list sizes (host to device), [512, 736) the
+// counters of a finished call (stage_stats).  Each is read only after a wait on the stream
+// that wrote it, and written only after the previous call's work on that stream finished.
+constexpr size_t kPinnedBytes = 1024;
 constexpr int kShortVariant = 9;   // variants 9, 10: dp_short (s16x2 unitary short pairs), 16 / 32 rows per thread
 constexpr int kVariants = kShortVariant + kShortFormCount;   // 0..8: dp_kernel (pa_kern_v*.cu)
 constexpr int kDefaultShortVariant = kShortVariant;          // with the rule below: 16 or 32 rows per thread
@@ -1310,9 +1315,11 @@ pa_status run_device(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const u
 
 // ---------------------------------------------------------------------------
 // roofline microkernel: the cell-update instruction mix of dp_kernel on
-// registers only (no memory, no shuffles), timed over the whole chip.
+// registers only (no memory, no shuffles), timed over the whole chip.  TRACK adds
+// what local scoring needs on top of the recurrence: the column maximum of the
+// thread's rows (three-operand max tree) and the test for a strict improvement.
 // ---------------------------------------------------------------------------
-template <class V>
+template <class V, bool TRACK = false>
 __global__ void __launch_bounds__(256) k_roofline(int steps, uint32_t seed, uint32_t *sink)
 {
     constexpr int R = 16;
@@ -1325,6 +1332,7 @@ __global__ void __launch_bounds__(256) k_roofline(int steps, uint32_t seed, uint
         Sel[k] = V::selector((k + threadIdx.x) & 3, (k * 3 + threadIdx.x) & 3);
     }
     uint32_t ta = 0x01fcfcfcu ^ (seed & 0x03000000u), tb = 0xfc01fcfcu, up = V::splat(2041), diag0 = V::splat(2048);
+    uint32_t best = V::splat(2048), moved = 0;
     for (int s = 0; s < steps; ++s) {
         uint32_t diag = diag0, Ed = up;
 #pragma unroll
@@ -1338,12 +1346,17 @@ __global__ void __launch_bounds__(256) k_roofline(int steps, uint32_t seed, uint
             Fr[k] = V::max2(V::subc(Fr[k], EXTA), hoe);
             Ed = V::max2(V::subc(Ed, EXTA), hoe);
         }
+        if (TRACK) {
+            const uint32_t nb = V::max2(best, tree_max<V, R>(H));
+            moved += (nb ^ best) != 0u;
+            best = nb;
+        }
         diag0 = H[R - 1];
         up = Ed;
         ta = (ta << 8) | (ta >> 24);
         tb = (tb >> 8) | (tb << 24);
     }
-    uint32_t acc = up;
+    uint32_t acc = up ^ best ^ moved;
 #pragma unroll
     for (int k = 0; k < R; ++k) acc ^= H[k] ^ Fr[k];
     if (acc == 0x12345678u) sink[blockIdx.x] = acc;
@@ -2139,35 +2152,36 @@ pa_status pa_measure_roofline(pa_ctx *ctx, pa_roofline *out)
     DevBuf sink;
     pa_status s = ensure(ctx, sink, 1 << 20);
     if (s) return s;
-    int per16 = 0, per32 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per16, k_roofline<L16>, 256, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per32, k_roofline<L32>, 256, 0);
+    int per[3] = {0, 0, 0};
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], k_roofline<L16>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], k_roofline<L32>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[2], k_roofline<L16, true>, 256, 0);
     const int steps = 4096;
-    double best16 = 0, best32 = 0;
+    double best[3] = {0, 0, 0};
     for (int rep = 0; rep < 4; ++rep) {
-        for (int w = 0; w < 2; ++w) {
-            const int per = w ? per32 : per16;
-            const int grid = std::max(1, per) * ctx->sm_count;
+        for (int w = 0; w < 3; ++w) {
+            const int grid = std::max(1, per[w]) * ctx->sm_count;
             PA_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-            if (w) k_roofline<L32><<<grid, 256, 0, ctx->stream>>>(steps, rep, (uint32_t *)sink.p);
+            if (w == 1) k_roofline<L32><<<grid, 256, 0, ctx->stream>>>(steps, rep, (uint32_t *)sink.p);
+            else if (w == 2) k_roofline<L16, true><<<grid, 256, 0, ctx->stream>>>(steps, rep, (uint32_t *)sink.p);
             else k_roofline<L16><<<grid, 256, 0, ctx->stream>>>(steps, rep, (uint32_t *)sink.p);
             PA_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
             PA_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
             float ms = 0;
             cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-            const double cells = (double)grid * 256 * steps * 16 * (w ? 1 : 2);
-            const double r = cells / (ms * 1e-3);
-            if (w) best32 = std::max(best32, r); else best16 = std::max(best16, r);
+            const double cells = (double)grid * 256 * steps * 16 * (w == 1 ? 1 : 2);
+            best[w] = std::max(best[w], cells / (ms * 1e-3));
         }
     }
     cudaFree(sink.p);
     int clk = 0;
     cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, ctx->device);
-    out->s16x2_cells_per_s = best16;
-    out->s32_cells_per_s = best32;
+    out->s16x2_cells_per_s = best[0];
+    out->s32_cells_per_s = best[1];
     out->sm_clock_mhz = clk / 1000.0;
     out->sm_count = ctx->sm_count;
     out->reserved = 0;
+    out->s16x2_local_cells_per_s = best[2];
     return PA_OK;
 }
 
