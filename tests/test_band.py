@@ -375,3 +375,38 @@ def test_gpu_learned_band_gains_over_straight_band():
     assert cert[1].sum() >= 0.6 * n_long, (int(cert[1].sum()), n_long)
     assert cert[2].sum() <= 0.1 * n_long, (int(cert[2].sum()), n_long)
     assert got[1]["band_rounds"][cert[1]].mean() <= 1.0        # round 0 or one doubling
+
+
+@pytest.mark.gpu
+def test_gpu_band_mode_device_entry_without_stats():
+    """Band mode through pa_align_batch_device without a stats block returns once its last
+    launches are queued; after a stream sync the results equal the plain path's, for a batch
+    with long pairs (band rounds, concurrent long and largest classes, full-DP leftovers) and
+    for one without (short pairs only), twice in a row on the same buffers."""
+    import os
+    import torch
+    import pairwise_aligner_gb300 as pa
+    from pairwise_aligner_gb300 import Aligner, band
+    dev = torch.device("cuda:0")
+    model = band.BandModel(device=dev)
+    model.load(os.path.join(os.path.dirname(pa.__file__), "data", "band_model.npz"))
+    for d in (workloads.config5(seed=91, n_pairs=512, strata=(0.4, 0.4, 0.2)),
+              workloads.config4(seed=92, n_pairs=1024)):
+        n = len(d["off1"]) - 1
+        base = dict(local=False, match=d["match"], mismatch=d["mismatch"], gap_open=d["gap_open"],
+                    gap_extension=d["gap_extension"], first_column_free=False, first_row_free=False,
+                    last_column_free=False, last_row_free=False, band_mode=0)
+        plain = Aligner(base).compute_arrays(d["seq1"], d["off1"], d["seq2"], d["off2"])
+        al = Aligner({**base, "band_mode": 1})
+        model.to_context(al.context)
+        tens = [torch.from_numpy(np.array(d["seq1"])).to(dev), torch.from_numpy(d["off1"].astype(np.int64)).to(dev),
+                torch.from_numpy(np.array(d["seq2"])).to(dev), torch.from_numpy(d["off2"].astype(np.int64)).to(dev)]
+        stream = torch.cuda.Stream(device=dev)
+        for _ in range(2):
+            out = torch.full((n * 16,), 0xCD, dtype=torch.uint8, device=dev)
+            al.compute_device(*tens, out, stream=stream)
+            torch.cuda.synchronize()
+            got = np.frombuffer(out.cpu().numpy().tobytes(), dtype=pa.RESULT_DTYPE)
+            for f in ("score", "end1", "end2"):
+                assert np.array_equal(got[f], plain[f]), f
+            assert ((got["flags"] & (BANDED | FULL | TRIVIAL)) != 0).all()
