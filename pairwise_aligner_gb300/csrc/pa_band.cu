@@ -2,7 +2,7 @@
 // (forward, backward, Adam), and the banded DP with its certificate.
 //
 // None of this has a counterpart in the reference (it has no banded or
-// heuristic mode); the full DP of pa_dp.cuh stays the exact fallback and judge.
+// heuristic mode); the full DP of pa_dp.cuh stays the exact fallback and arbiter.
 //
 // Features (k_kmer_hist): a 128-bin histogram of the diagonal offsets j - i of
 // 12-mers shared by sequence1 (position i) and sequence2 (position j), bins
