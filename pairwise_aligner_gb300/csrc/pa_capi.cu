@@ -35,12 +35,10 @@ constexpr int64_t kDefaultRingM = 65536;   // device entry points: CTA mode up t
 constexpr int kDefaultG = 8;       // threads per group
 // Page-locked host words of a context: [0, 8) band mode's bad-offset count, [16, 80) class
 // ranges, [80, 144) class counts, [160, 224) the two band steps' totals, [224, 236) the long
-// full-DP routing counts, [256, 280) full-DP list sizes (host to device), and from 512 one
-// 256-byte slot per chunk of a host call with the counters of that chunk's DP (stage_stats).
-// Each is read only after a wait on the stream that wrote it, and written only after the
-// previous call's work on that stream finished.
-constexpr size_t kPinnedBytes = 2048;
-constexpr int kMaxChunks = 4;           // host calls copy and align in up to this many chunks
+// full-DP routing counts, [256, 280) full-DP list sizes (host to device), [512, 736) the
+// counters of a finished call (stage_stats).  Each is read only after a wait on the stream
+// that wrote it, and written only after the previous call's work on that stream finished.
+constexpr size_t kPinnedBytes = 1024;
 constexpr int kShortVariant = 9;   // variants 9, 10: dp_short (s16x2 unitary short pairs), 16 / 32 rows per thread
 constexpr int kVariants = kShortVariant + kShortFormCount;   // 0..8: dp_kernel (pa_kern_v*.cu)
 constexpr int kDefaultShortVariant = kShortVariant;          // with the rule below: 16 or 32 rows per thread
@@ -78,9 +76,7 @@ struct pa_ctx {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaStream_t side2 = nullptr;                     // team kernels run beside the CTA kernels
     cudaEvent_t ev_join2 = nullptr;
-    uint8_t *pinned = nullptr;                        // page-locked host words (layout at kPinnedBytes)
-    cudaEvent_t ev_copy[2 * kMaxChunks] = {};         // chunked host calls: a chunk's two copies done
-    uint64_t hint_pairs = 0, hint_b1 = 0, hint_b2 = 0; // whole-batch sizes for a chunk's tuning choice
+    uint8_t *pinned = nullptr;                        // page-locked host words for band mode's reads
     pa_options opt{};
     std::string err;
     // device work buffers (grow only)
@@ -608,11 +604,6 @@ int rule_group_threads(const pa_ctx *c, uint64_t n_pairs, int lanes)
 void apply_tuning(pa_ctx *c, const pa_config *cfg, uint64_t n_pairs, uint64_t b1, uint64_t b2)
 {
     if (!cfg) return;
-    if (c->hint_pairs) {                              // a chunk of a larger host call
-        n_pairs = c->hint_pairs;
-        b1 = c->hint_b1;
-        b2 = c->hint_b2;
-    }
     const int mi = (cfg->method & ~PA_SCORE_MATRIX) == PA_METHOD_LOCAL ? 0 : 1;
     const pa_tune_entry &e = c->tuning.s16[mi][tune_size_class(n_pairs)][tune_shape_class(n_pairs, b1, b2)];
     if (!c->fixed_variant) {
@@ -664,8 +655,8 @@ pa_status band_predict(pa_ctx *c, const DpParams &P, const uint8_t *s1, const ui
     return PA_OK;
 }
 
-pa_status read_stats(pa_ctx *c, pa_stats *stats, bool staged = false, int slot = 0);
-void stage_stats(pa_ctx *c, cudaStream_t st, int slot = 0);
+pa_status read_stats(pa_ctx *c, pa_stats *stats, bool staged = false);
+void stage_stats(pa_ctx *c, cudaStream_t st);
 
 // Band mode (host-synchronous between rounds): classify and sort as the plain
 // path, build every pair's band, then per round and work class: windows ->
@@ -1202,24 +1193,22 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
 
 // Queue the copies of the call's counters into page-locked host words (read_stats with
 // staged = true reads them after the caller's wait on `st`).
-constexpr size_t kPinStats = 512;      // per slot: PrepStats, then 16 counter words
-void stage_stats(pa_ctx *c, cudaStream_t st, int slot)
+constexpr size_t kPinStats = 512;      // PrepStats, then 16 counter words
+void stage_stats(pa_ctx *c, cudaStream_t st)
 {
-    static_assert(kPinStats + 256 * (kMaxChunks - 1) + sizeof(PrepStats) + 64 <= kPinnedBytes, "page-locked words");
-    uint8_t *dst = c->pinned + kPinStats + 256 * slot;
-    cudaMemcpyAsync(dst, c->pstats.p, sizeof(PrepStats), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(dst + sizeof(PrepStats), c->counters.p, 64, cudaMemcpyDeviceToHost, st);
+    static_assert(kPinStats + sizeof(PrepStats) + 64 <= kPinnedBytes, "page-locked words");
+    cudaMemcpyAsync(c->pinned + kPinStats, c->pstats.p, sizeof(PrepStats), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->pinned + kPinStats + sizeof(PrepStats), c->counters.p, 64, cudaMemcpyDeviceToHost, st);
 }
 
 // Counters of the finished call (after a sync): class sizes, reruns, error bits.
-pa_status read_stats(pa_ctx *c, pa_stats *stats, bool staged, int slot)
+pa_status read_stats(pa_ctx *c, pa_stats *stats, bool staged)
 {
     PrepStats ps;
     uint32_t ctr[16];
     if (staged) {
-        const uint8_t *src = c->pinned + kPinStats + 256 * slot;
-        std::memcpy(&ps, src, sizeof(ps));
-        std::memcpy(ctr, src + sizeof(PrepStats), sizeof(ctr));
+        std::memcpy(&ps, c->pinned + kPinStats, sizeof(ps));
+        std::memcpy(ctr, c->pinned + kPinStats + sizeof(PrepStats), sizeof(ctr));
     } else {
         PA_CUDA(c, cudaMemcpy(&ps, c->pstats.p, sizeof(ps), cudaMemcpyDeviceToHost));
         PA_CUDA(c, cudaMemcpy(ctr, c->counters.p, sizeof(ctr), cudaMemcpyDeviceToHost));
@@ -1426,12 +1415,6 @@ pa_status pa_create(pa_ctx **out, int device_ordinal, const pa_options *options)
         pa_destroy(c);
         return PA_ERR_CUDA;
     }
-    for (cudaEvent_t &e : c->ev_copy)
-        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
-            cudaGetLastError();
-            pa_destroy(c);
-            return PA_ERR_CUDA;
-        }
     // defaults measured on GB300 (262,144 pairs of 64..512 bp): local s16x2 is fastest with
     // variant 7, global with variant 4; 8 lanes per group
     c->tuning = pa_tuning{};
@@ -1487,8 +1470,6 @@ pa_status pa_destroy(pa_ctx *c)
     if (c->side2) cudaStreamDestroy(c->side2);
     if (c->ev_join2) cudaEventDestroy(c->ev_join2);
     if (c->pinned) cudaFreeHost(c->pinned);
-    for (cudaEvent_t e : c->ev_copy)
-        if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return PA_OK;
@@ -1702,77 +1683,6 @@ static pa_status align_host(pa_ctx *ctx, const pa_config *config, const uint8_t 
     const uint64_t *h1 = off1, *h2 = off2;
     if (base1) { r1.assign(off1, off1 + n_pairs + 1); for (auto &v : r1) v -= base1; h1 = r1.data(); }
     if (base2) { r2.assign(off2, off2 + n_pairs + 1); for (auto &v : r2) v -= base2; h2 = r2.data(); }
-    // Large plain calls copy and align in chunks of pairs: the bytes of chunk k + 1 cross while
-    // chunk k is aligned.  Each chunk is one run_device call on its slice of the staged batch,
-    // with the kernel choice of the whole batch; its counters are staged for the error check.
-    const bool chunked = !packed && !(config && config->band_mode) && !stats && !bands &&
-                         n_pairs >= (1u << 17) && b1 + b2 >= (64ull << 20);
-    if (chunked) {
-        const int K = kMaxChunks;
-        uint64_t cut[kMaxChunks + 1];
-        cut[0] = 0;
-        cut[K] = n_pairs;
-        for (int k = 1; k < K; ++k) {                 // about equal bytes per chunk
-            const uint64_t want = (b1 + b2) * k / K;
-            uint64_t lo = cut[k - 1], hi = n_pairs;
-            while (lo < hi) {
-                const uint64_t mid = (lo + hi) / 2;
-                if ((h1[mid] - h1[0]) + (h2[mid] - h2[0]) < want) lo = mid + 1; else hi = mid;
-            }
-            cut[k] = lo;
-        }
-        PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off1.p, h1, (n_pairs + 1) * 8, cudaMemcpyHostToDevice, st));
-        PA_CUDA(ctx, cudaMemcpyAsync(ctx->in_off2.p, h2, (n_pairs + 1) * 8, cudaMemcpyHostToDevice, st));
-        PA_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
-        PA_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-        PA_CUDA(ctx, cudaStreamWaitEvent(ctx->side2, ctx->ev_fork, 0));
-        for (int k = 0; k < K; ++k) {
-            const uint64_t a1 = h1[cut[k]], e1 = h1[cut[k + 1]], a2 = h2[cut[k]], e2 = h2[cut[k + 1]];
-            if (e1 > a1)
-                PA_CUDA(ctx, cudaMemcpyAsync((uint8_t *)ctx->in_seq1.p + a1, seq1 + base1 + a1, e1 - a1,
-                                             cudaMemcpyHostToDevice, ctx->side));
-            if (e2 > a2)
-                PA_CUDA(ctx, cudaMemcpyAsync((uint8_t *)ctx->in_seq2.p + a2, seq2 + base2 + a2, e2 - a2,
-                                             cudaMemcpyHostToDevice, ctx->side2));
-            PA_CUDA(ctx, cudaEventRecord(ctx->ev_copy[2 * k], ctx->side));
-            PA_CUDA(ctx, cudaEventRecord(ctx->ev_copy[2 * k + 1], ctx->side2));
-        }
-        // the offsets' check and the longest block-mode sequence1, while the copies run
-        int64_t long_m = 0;
-        for (uint64_t k = 0; k < n_pairs; ++k) {
-            if (off1[k + 1] < off1[k] || off2[k + 1] < off2[k]) {
-                PA_CUDA(ctx, cudaDeviceSynchronize());
-                return fail(ctx, PA_ERR_INVALID_ARGUMENT, "offsets must be non-decreasing");
-            }
-            const int64_t m = (int64_t)(off1[k + 1] - off1[k]), n = (int64_t)(off2[k + 1] - off2[k]);
-            if (m * n >= ctx->long_cells) long_m = std::max(long_m, m);
-        }
-        ctx->want_ring_m = long_m;
-        ctx->hint_pairs = n_pairs;
-        ctx->hint_b1 = b1;
-        ctx->hint_b2 = b2;
-        for (int k = 0; k < K; ++k) {
-            const uint64_t p0 = cut[k], np = cut[k + 1] - p0;
-            if (!np) continue;
-            PA_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_copy[2 * k], 0));
-            PA_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_copy[2 * k + 1], 0));
-            s = run_device(ctx, config, (const uint8_t *)ctx->in_seq1.p, (const uint64_t *)ctx->in_off1.p + p0, b1,
-                           (const uint8_t *)ctx->in_seq2.p, (const uint64_t *)ctx->in_off2.p + p0, b2, np,
-                           (pa_result *)ctx->in_out.p + p0, nullptr, false);
-            if (s) {
-                ctx->hint_pairs = 0;
-                PA_CUDA(ctx, cudaDeviceSynchronize());
-                return s;
-            }
-            stage_stats(ctx, st, k);
-        }
-        ctx->hint_pairs = 0;
-        PA_CUDA(ctx, cudaMemcpyAsync(out, ctx->in_out.p, n_pairs * sizeof(pa_result), cudaMemcpyDeviceToHost, st));
-        PA_CUDA(ctx, cudaStreamSynchronize(st));
-        for (int k = 0; k < K; ++k)
-            if (cut[k + 1] > cut[k] && (s = read_stats(ctx, nullptr, true, k))) return s;
-        return PA_OK;
-    }
     // the two sequence sets go over two copy engines at once (side stream joins before the DP)
     PA_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
     PA_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));

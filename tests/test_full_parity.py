@@ -57,11 +57,6 @@ def test_every_local_pair_of_the_262144_pair_batch(pa, oracle):
     res = al.compute_arrays(d["seq1"], d["off1"], d["seq2"], d["off2"])
     assert len(res) == 262144
     _assert_exact(oracle, d, res)
-    # without a stats block the host entry copies and aligns this batch in chunks (the copy of
-    # one chunk overlapping the alignment of the previous one): the same results
-    chunked = al.compute_arrays(d["seq1"], d["off1"], d["seq2"], d["off2"], stats=False)
-    for f in ("score", "end1", "end2", "flags"):
-        assert np.array_equal(chunked[f], res[f]), f"chunked host call: {f} differs"
 
 
 def test_every_long_read_pair_of_the_8192_pair_batch(pa, oracle):
