@@ -10,7 +10,7 @@ constexpr int kRowsCl = 16;
 template <class V, int MODE, bool GEN>
 void *cluster_fn()
 {
-    return (void *)dp_kernel_cluster<V, kRowsCl, MODE, GEN, MODE == M_LOCAL ? 36 : 44, kClusterBlocks>;
+    return (void *)dp_kernel_cluster<V, kRowsCl, MODE, GEN, 36, kClusterBlocks>;
 }
 
 void *pick(bool lanes16, bool gen, int mode)

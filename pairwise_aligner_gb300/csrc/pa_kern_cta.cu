@@ -16,7 +16,7 @@ int occ_cta()
     static int per_sm = -1;
     if (per_sm < 0) {
         int v = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel_cta<V, kRowsCta, MODE, GEN, MODE == M_LOCAL ? 36 : 44>,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, dp_kernel_cta<V, kRowsCta, MODE, GEN, 36>,
                                                       kBlock, 0);
         per_sm = v < 1 ? 1 : v;
     }
@@ -26,7 +26,7 @@ int occ_cta()
 template <class V, int MODE, bool GEN>
 void go_cta(int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
 {
-    dp_kernel_cta<V, kRowsCta, MODE, GEN, MODE == M_LOCAL ? 36 : 44><<<grid, kBlock, 0, st>>>(L, P);
+    dp_kernel_cta<V, kRowsCta, MODE, GEN, 36><<<grid, kBlock, 0, st>>>(L, P);
 }
 
 // Teams of kTeam warps per unit (two units per block) for block-mode pairs with few passes.
@@ -39,7 +39,7 @@ int occ_team()
     if (per_sm < 0) {
         int v = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &v, dp_kernel_team<V, kRowsCta, MODE, GEN, MODE == M_LOCAL ? 36 : 44, kTeam>, kBlock, 0);
+            &v, dp_kernel_team<V, kRowsCta, MODE, GEN, 36, kTeam>, kBlock, 0);
         per_sm = v < 1 ? 1 : v;
     }
     return per_sm;
@@ -48,7 +48,7 @@ int occ_team()
 template <class V, int MODE, bool GEN>
 void go_team(int grid, cudaStream_t st, const DpLaunch &L, const DpParams &P)
 {
-    dp_kernel_team<V, kRowsCta, MODE, GEN, MODE == M_LOCAL ? 36 : 44, kTeam><<<grid, kBlock, 0, st>>>(L, P);
+    dp_kernel_team<V, kRowsCta, MODE, GEN, 36, kTeam><<<grid, kBlock, 0, st>>>(L, P);
 }
 
 template <class V, bool GEN>
