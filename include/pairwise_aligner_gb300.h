@@ -295,7 +295,7 @@ typedef struct pa_band_options {
     float margin;               /* default 1.25 */
     int32_t w_min;              /* default 16   */
     int32_t straight_w0;        /* default 64   */
-    float full_frac;            /* default 0.75 */
+    float full_frac;            /* default 0.85 */
     int32_t max_rounds;         /* default 2    */
     float team_full_frac;       /* default 0.65 */
     int32_t reserved[2];

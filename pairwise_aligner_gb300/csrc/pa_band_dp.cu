@@ -312,7 +312,7 @@ __global__ void k_mark_full(pa_result *__restrict__ out, uint64_t n_pairs)
 
 // ---- host-side launchers ---------------------------------------------------------
 namespace {
-constexpr int kBandVar = 12;     // branch-free top input + two-op vertical-gap chain
+constexpr int kBandVar = 36;     // branch-free top input, one-op vertical-gap chain, no table prefetch
 
 template <class V, bool CTA>
 int band_occ()

@@ -101,7 +101,7 @@ struct pa_ctx {
     uint64_t graph_clock = 0;
     uint64_t last_launches = 0;
     // band mode
-    pa_band_options band_opt{1.25f, 16, 64, 0.75f, 2, 0.65f, {0, 0}};
+    pa_band_options band_opt{1.25f, 16, 64, 0.85f, 2, 0.65f, {0, 0}};
     DevBuf band_spec, band_win, band_code, band_bsum, band_ctr, band_in;
     DevBuf band_list[22];
     DevBuf mlp_w[6], mlp_feat, mlp_x, mlp_h1, mlp_h2, mlp_out;
