@@ -39,7 +39,6 @@ constexpr int kDefaultG = 8;       // threads per group
 // counters of a finished call (stage_stats).  Each is read only after a wait on the stream
 // that wrote it, and written only after the previous call's work on that stream finished.
 constexpr size_t kPinnedBytes = 1024;
-constexpr uint32_t kGroupSlotCap = 2048;   // short-pair units up to this sequence1 length use group regions
 constexpr int kShortVariant = 9;   // variants 9, 10: dp_short (s16x2 unitary short pairs), 16 / 32 rows per thread
 constexpr int kVariants = kShortVariant + kShortFormCount;   // 0..8: dp_kernel (pa_kern_v*.cu)
 constexpr int kDefaultShortVariant = kShortVariant;          // with the rule below: 16 or 32 rows per thread
@@ -82,7 +81,6 @@ struct pa_ctx {
     std::string err;
     // device work buffers (grow only)
     DevBuf keys, order, hist, starts, cursor, sums, ranges, counts, qtab, boundary, rerun, counters, pstats;
-    DevBuf group_slots;               // short-pair kernel: a reusable slot region per resident group
     DevBuf slots;                 // short-pair kernel: 16-byte column slots, (seq1_bytes + n_pairs)
     DevBuf ring, rerun_long;      // CTA mode: boundary rows per block; s16 long pairs to redo in s32
     int32_t ring_m = 0;           // longest sequence1 the ring rows hold (0: no CTA mode yet)
@@ -423,10 +421,6 @@ pa_status enqueue(pa_ctx *c, const pa_config *cfg, const DpParams &P, const Clas
     L.out = out;
     L.boundary = (Cell *)c->boundary.p;
     L.slots = (Slot *)c->slots.p;
-    L.group_slots = c->group_slots.p ? (Slot *)c->group_slots.p : nullptr;
-    L.group_cap = (uint32_t)(c->group_slots.cap / ((size_t)2 * c->sm_count * (kBlock / std::max(1, c->G[K_S16])) *
-                                                    sizeof(Slot))) - 1;
-    L.max_m = &((const PrepStats *)c->pstats.p)->max_m_s16;
     L.spin_limit = c->wait_limit;
     L.rerun_list = (uint32_t *)c->rerun.p;
     L.rerun_count = counters + 4;
@@ -577,12 +571,6 @@ pa_status prepare_buffers(pa_ctx *c, uint64_t n_pairs, uint64_t b1)
     if ((s = ensure(c, c->qtab, (b1 + np) * 4))) return s;
     if ((s = ensure(c, c->boundary, (b1 + np) * sizeof(Cell)))) return s;
     if ((s = ensure(c, c->slots, (b1 + np) * sizeof(Slot)))) return s;
-    // the short-pair kernel's per-group regions: at most 2 resident blocks per SM (its launch
-    // bounds), kBlock / G groups each, kGroupSlotCap + 1 slots per group
-    const int g = c->G[K_S16];
-    if (c->variant[K_S16] >= kShortVariant && dp_short_supports(g) &&
-        (s = ensure(c, c->group_slots, (size_t)2 * c->sm_count * (kBlock / g) * (kGroupSlotCap + 1) * sizeof(Slot))))
-        return s;
     return PA_OK;
 }
 
@@ -731,10 +719,6 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
     L.out = out;
     L.boundary = (Cell *)c->boundary.p;
     L.slots = (Slot *)c->slots.p;
-    L.group_slots = c->group_slots.p ? (Slot *)c->group_slots.p : nullptr;
-    L.group_cap = (uint32_t)(c->group_slots.cap / ((size_t)2 * c->sm_count * (kBlock / std::max(1, c->G[K_S16])) *
-                                                    sizeof(Slot))) - 1;
-    L.max_m = &((const PrepStats *)c->pstats.p)->max_m_s16;
     L.band_win = (const int2 *)c->band_win.p;
     L.band = spec;
     L.band_code = (uint8_t *)c->band_code.p;
@@ -1461,7 +1445,7 @@ pa_status pa_destroy(pa_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     drop_graphs(c);
     DevBuf *bufs[] = {&c->keys, &c->order, &c->hist, &c->starts, &c->cursor, &c->sums, &c->ranges,
-                      &c->counts, &c->qtab, &c->boundary, &c->slots, &c->group_slots, &c->rerun, &c->counters, &c->pstats,
+                      &c->counts, &c->qtab, &c->boundary, &c->slots, &c->rerun, &c->counters, &c->pstats,
                       &c->in_seq1, &c->in_off1, &c->in_seq2, &c->in_off2, &c->in_out,
                       &c->band_spec, &c->band_win, &c->band_code, &c->band_bsum, &c->band_ctr, &c->band_in,
                       &c->mlp_feat, &c->mlp_x, &c->mlp_h1, &c->mlp_h2, &c->mlp_out,

@@ -104,13 +104,8 @@ struct DpLaunch {
     const int8_t *rank_map;
     const int32_t *matrix;
     int32_t mdim;
-    // short-pair kernel (pa_short.cuh): (seq1_bytes + n_pairs) column slots, pair k's at off1[k] + k;
-    // or, when the class's longest sequence1 (*max_m) is at most group_cap, one region of
-    // group_cap + 1 slots per resident group, reused unit after unit (it stays in L2)
+    // short-pair kernel (pa_short.cuh): (seq1_bytes + n_pairs) column slots, pair k's at off1[k] + k
     Slot *slots;
-    Slot *group_slots;
-    const unsigned long long *max_m;
-    uint32_t group_cap;
     // CTA / team / cluster modes: polls a progress wait makes after its first look before it
     // gives up (pa_set_wait_limit; default 2^24)
     uint32_t spin_limit;

@@ -32,7 +32,6 @@ struct PrepStats {
     unsigned long long overflow;    // pairs whose int32 bound fails
     unsigned long long invalid;     // substitution-matrix scoring: pairs with a symbol outside it
     unsigned long long bad_offsets; // pairs whose offsets are decreasing or run past the byte buffers
-    unsigned long long max_m_s16;   // the longest sequence1 of class K_S16
 };
 
 // Result of a pair the DP does not compute (no valid score): INT32_MIN at (0, 0).
@@ -101,7 +100,7 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
     __shared__ unsigned long long sh[19];
     if (threadIdx.x < 19) sh[threadIdx.x] = 0;
     __syncthreads();
-    unsigned long long my_cells = 0, my_overflow = 0, my_bad = 0, my_max_m = 0;
+    unsigned long long my_cells = 0, my_overflow = 0, my_bad = 0;
     for (uint64_t p = warp; p < n_pairs; p += nwarps) {
         const uint64_t q0 = off1[p], q1 = off1[p + 1], t0 = off2[p], t1 = off2[p + 1];
         if (q0 > q1 || q1 > seq1_bytes || t0 > t1 || t1 > seq2_bytes) {
@@ -182,19 +181,14 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
                 key = (klass << kClassShift) | (quant_shape(shape > 0xffffffffull ? 0xffffffffu : (uint32_t)shape) << 10) |
                       quant_len((uint32_t)m);
                 my_cells += (unsigned long long)(m * n);
-                if (klass == K_S16 && (unsigned long long)m > my_max_m) my_max_m = (unsigned long long)m;
             }
             keys[p] = key;
             atomicAdd(&hist[key], 1u);
             atomicAdd(&sh[1 + klass], 1ull);
         }
     }
-    __shared__ unsigned long long sh_max_m;
-    if (threadIdx.x == 0) sh_max_m = 0;
-    __syncthreads();
     if (lane == 0) {
         if (my_cells) atomicAdd(&sh[0], my_cells);
-        if (my_max_m) atomicMax(&sh_max_m, my_max_m);
         if (my_overflow) atomicAdd(&sh[17], my_overflow);
         if (my_bad) atomicAdd(&sh[18], my_bad);
     }
@@ -205,7 +199,6 @@ __global__ void k_classify(const uint8_t *__restrict__ seq1, const uint64_t *__r
             if (sh[1 + k]) atomicAdd(&st->n_class[k], sh[1 + k]);
         if (sh[17]) atomicAdd(&st->overflow, sh[17]);
         if (sh[18]) atomicAdd(&st->bad_offsets, sh[18]);
-        if (sh_max_m) atomicMax(&st->max_m_s16, sh_max_m);
     }
 }
 

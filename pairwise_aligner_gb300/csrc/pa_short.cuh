@@ -240,10 +240,6 @@ __global__ void __launch_bounds__(kBlock, 2) dp_short(DpLaunch L, DpParams P)
     const uint32_t n_units = (count + ppw - 1) / ppw;
     const uint32_t match4 = (uint8_t)(P.match - P.shift) * 0x01010101u;
     const uint32_t mis4 = (uint8_t)(P.mismatch - P.shift) * 0x01010101u;
-    // the group's own slot region when every unit of the class fits in it
-    const bool grouped = L.group_slots && *L.max_m <= (unsigned long long)L.group_cap;
-    Slot *const my_slots = grouped ? L.group_slots + (size_t)(blockIdx.x * NGROUPS + threadIdx.x / G) * (L.group_cap + 1)
-                                   : nullptr;
 
     for (;;) {
         uint32_t uu = 0;
@@ -268,7 +264,7 @@ __global__ void __launch_bounds__(kBlock, 2) dp_short(DpLaunch L, DpParams P)
             u.nh = max(u.n[0], u.n[1]);
             u.passes = (u.nh + G * R - 1) / (G * R);
             const uint32_t owner = u.m[1] > u.m[0] ? u.id[1] : u.id[0];
-            u.slot = grouped ? my_slots : L.slots + (L.off1[owner] + owner);   // slots 0..ms
+            u.slot = L.slots + (L.off1[owner] + owner);   // slots 0..m(owner) = 0..ms
             su = u;
         }
         for (int l = 0; l < 2; ++l) {
