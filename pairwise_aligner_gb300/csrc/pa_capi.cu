@@ -920,9 +920,14 @@ pa_status run_band(pa_ctx *c, const pa_config *cfg, const uint8_t *s1, const uin
         PA_CUDA(c, cudaStreamSynchronize(st));
         nfull[S.k] += h[0];
         S.nb = h[1];
-        // CTA mode: a team of warps per pair sized to the passes a window keeps in flight
+        // CTA mode: a team of warps per pair, at most half the passes a window keeps in flight
+        // (a window of W columns keeps about W / rows passes going); more pairs with fewer
+        // warps each beat fewer pairs with waiting warps.  Measured on 262,144 config-5 pairs:
+        // for the 1,000-10,000-base class (mean window 1,600-2,500 columns) one warp per pair
+        // was 1-2 % faster than two or four and eight was 1.30x slower; for the largest pairs
+        // (mean window 8,900-14,800) eight warps were 1.16x faster than four, 1.83x than two
         const double mean_width = w[1] ? (double)w[0] / (double)w[1] : 0.0;
-        S.team = mean_width >= 8.0 * B.rows ? 8 : mean_width >= 4.0 * B.rows ? 4 : mean_width >= 2.0 * B.rows ? 2 : 1;
+        S.team = mean_width >= 16.0 * B.rows ? 8 : mean_width >= 8.0 * B.rows ? 4 : mean_width >= 4.0 * B.rows ? 2 : 1;
         return PA_OK;
     };
     auto step_dp = [&](Step &S, int r) -> pa_status {
